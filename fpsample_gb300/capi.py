@@ -1,0 +1,161 @@
+"""ctypes view of libfpsgpu's C ABI (include/fpsgpu.h).
+
+For callers that hold device buffers (for example torch CUDA tensors) or want
+to call the C entry points directly from Python.  Everything here runs on the
+GPU; failures raise ``FpsGpuError`` with the library's code and message.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfpsgpu.so")
+
+_sz = ctypes.c_size_t
+_vp = ctypes.c_void_p
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_f32p = ctypes.POINTER(ctypes.c_float)
+_szp = ctypes.POINTER(ctypes.c_size_t)
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "bucket_fps_kdline": (ctypes.c_int, [_f32p, _sz, _sz, _sz, _sz, _sz, _szp]),
+    "fpsgpu_fps": (ctypes.c_int, [_f32p, _sz, _sz, _sz, _szp, _sz, _szp]),
+    "fpsgpu_kdline_device": (ctypes.c_int, [_vp, _sz, _sz, _sz, _sz, _sz, _vp, _vp, _vp]),
+    "fpsgpu_fps_device": (ctypes.c_int, [_vp, _sz, _sz, _sz, _szp, _sz, _vp, _vp, _vp]),
+    "fpsgpu_kdline_build": (ctypes.c_int, [_f32p, _sz, _sz, _sz, _u64p, _u64p, _szp]),
+    "fpsgpu_set_fp_mode": (ctypes.c_int, [ctypes.c_int]),
+    "fpsgpu_get_fp_mode": (ctypes.c_int, []),
+    "fpsgpu_last_error": (ctypes.c_char_p, []),
+    "fpsgpu_version": (ctypes.c_char_p, []),
+}
+
+FP_MODES = {"nofma": 0, "fma": 1}
+
+
+class FpsGpuError(RuntimeError):
+    def __init__(self, fn: str, code: int, msg: str):
+        super().__init__(f"{fn} failed with error code {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is not built (python -m fpsample_gb300._build)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(fn: str, rc: int) -> None:
+    if rc != 0:
+        raise FpsGpuError(fn, rc, lib().fpsgpu_last_error().decode())
+
+
+def _rows(pc) -> np.ndarray:
+    a = np.ascontiguousarray(pc, dtype=np.float32)
+    if a.ndim != 2:
+        raise ValueError("points must be 2D")
+    return a
+
+
+def set_fp_mode(mode: str) -> None:
+    _check("fpsgpu_set_fp_mode", lib().fpsgpu_set_fp_mode(FP_MODES[mode]))
+
+
+def get_fp_mode() -> str:
+    return {v: k for k, v in FP_MODES.items()}[lib().fpsgpu_get_fp_mode()]
+
+
+def bucket_fps_kdline(pc, n_samples: int, start_idx: int, height: int) -> np.ndarray:
+    """The reference-compatible C entry point, host buffers."""
+    a = _rows(pc)
+    out = np.zeros(n_samples, np.uint64)
+    rc = lib().bucket_fps_kdline(a.ctypes.data_as(_f32p), a.shape[0], a.shape[1], n_samples,
+                                 start_idx, height, out.ctypes.data_as(_szp))
+    _check("bucket_fps_kdline", rc)
+    return out
+
+
+def fps(pc, n_samples: int, starts) -> np.ndarray:
+    a = _rows(pc)
+    st = np.atleast_1d(np.asarray(starts, dtype=np.uint64))
+    out = np.zeros(n_samples, np.uint64)
+    rc = lib().fpsgpu_fps(a.ctypes.data_as(_f32p), a.shape[0], a.shape[1], n_samples,
+                          st.ctypes.data_as(_szp), st.size, out.ctypes.data_as(_szp))
+    _check("fpsgpu_fps", rc)
+    return out
+
+
+def kdline_build(pc, height: int):
+    a = _rows(pc)
+    n = a.shape[0]
+    perm = np.zeros(n, np.uint64)
+    bst = np.zeros(n, np.uint64)
+    nb = _sz(0)
+    rc = lib().fpsgpu_kdline_build(a.ctypes.data_as(_f32p), n, a.shape[1], height,
+                                   perm.ctypes.data_as(_u64p), bst.ctypes.data_as(_u64p),
+                                   ctypes.byref(nb))
+    _check("fpsgpu_kdline_build", rc)
+    return perm, bst[: nb.value].copy()
+
+
+def kdline_device(points_ptr: int, n: int, dim: int, n_samples: int, start_idx: int, height: int,
+                  out_ptr: int, trace_ptr: int = 0, stream: int = 0) -> None:
+    """Device pointers (e.g. tensor.data_ptr()); out: n_samples uint64 (int64 tensor)."""
+    rc = lib().fpsgpu_kdline_device(points_ptr, n, dim, n_samples, start_idx, height, out_ptr,
+                                    trace_ptr or None, stream or None)
+    _check("fpsgpu_kdline_device", rc)
+
+
+def fps_device(points_ptr: int, n: int, dim: int, n_samples: int, starts, out_ptr: int,
+               trace_ptr: int = 0, stream: int = 0) -> None:
+    st = np.atleast_1d(np.asarray(starts, dtype=np.uint64))
+    rc = lib().fpsgpu_fps_device(points_ptr, n, dim, n_samples, st.ctypes.data_as(_szp), st.size,
+                                 out_ptr, trace_ptr or None, stream or None)
+    _check("fpsgpu_fps_device", rc)
+
+
+def kdline_tensor(points, n_samples: int, height: int, start_idx: int = 0, trace: bool = False):
+    """torch CUDA tensor [N, D] float32 in, int64 CUDA tensor [K] out (same values
+    as the uint64 indices), on the tensor's device and torch's current stream."""
+    import torch
+
+    pts = points.contiguous()
+    if pts.dtype != torch.float32 or not pts.is_cuda or pts.dim() != 2:
+        raise ValueError("points must be a 2D float32 CUDA tensor")
+    out = torch.empty(n_samples, dtype=torch.int64, device=pts.device)
+    tr = torch.empty(n_samples, dtype=torch.float32, device=pts.device) if trace else None
+    with torch.cuda.device(pts.device):
+        stream = torch.cuda.current_stream().cuda_stream
+        kdline_device(pts.data_ptr(), pts.shape[0], pts.shape[1], n_samples, start_idx, height,
+                      out.data_ptr(), tr.data_ptr() if trace else 0, stream)
+    return (out, tr) if trace else out
+
+
+def fps_tensor(points, n_samples: int, starts=0, trace: bool = False):
+    """torch CUDA tensor [N, D] float32 in, int64 CUDA tensor [K] out."""
+    import torch
+
+    pts = points.contiguous()
+    if pts.dtype != torch.float32 or not pts.is_cuda or pts.dim() != 2:
+        raise ValueError("points must be a 2D float32 CUDA tensor")
+    out = torch.empty(n_samples, dtype=torch.int64, device=pts.device)
+    tr = torch.empty(n_samples, dtype=torch.float32, device=pts.device) if trace else None
+    with torch.cuda.device(pts.device):
+        stream = torch.cuda.current_stream().cuda_stream
+        fps_device(pts.data_ptr(), pts.shape[0], pts.shape[1], n_samples, starts, out.data_ptr(),
+                   tr.data_ptr() if trace else 0, stream)
+    return (out, tr) if trace else out

@@ -1,0 +1,389 @@
+// C ABI of libfpsgpu (declared in include/fpsgpu.h) and the non-template
+// device helpers shared by the kernel translation units.
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fpsgpu_device.cuh"
+#include "fpsgpu_internal.h"
+#include "kdline.cuh"
+
+static_assert(sizeof(size_t) == sizeof(uint64_t), "size_t must be 64-bit");
+
+#define FPSGPU_VERSION_STRING "1.0.2+gb300.0.1"
+
+namespace fpsgpu {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+namespace {
+thread_local std::string t_last_error;
+}
+
+int set_error(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    t_last_error = buf;
+    return code;
+}
+
+void clear_error() { t_last_error.clear(); }
+
+// ---------------------------------------------------------------------------
+// device context: SM count and one non-blocking stream per device
+// ---------------------------------------------------------------------------
+namespace {
+std::mutex g_ctx_mu;
+std::vector<DevCtx> g_ctx;  // indexed by device ordinal; stream == nullptr until set up
+}
+
+int current_ctx(DevCtx* out) {
+    int dev = 0;
+    FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    if ((int)g_ctx.size() <= dev) g_ctx.resize(dev + 1);
+    DevCtx& c = g_ctx[dev];
+    if (c.stream == nullptr) {
+        int sms = 0;
+        FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        cudaStream_t s;
+        FPSGPU_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        c.device = dev;
+        c.sms = sms;
+        c.stream = s;
+    }
+    *out = c;
+    return FPSGPU_OK;
+}
+
+int launch_persistent(const void* func, int grid, int block, void** args, size_t smem,
+                      cudaStream_t stream, bool cooperative) {
+    if (cooperative) {
+        int dev = 0, sms = 0, per_sm = 0;
+        FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
+        FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        FPSGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, block, smem));
+        if ((long long)per_sm * sms < grid)
+            return set_error(FPSGPU_ERR_CUDA,
+                             "persistent grid of %d CTAs cannot be co-resident (%d per SM x %d SMs)",
+                             grid, per_sm, sms);
+        FPSGPU_CUDA_TRY(cudaLaunchCooperativeKernel(func, dim3(grid), dim3(block), args, smem, stream));
+    } else {
+        FPSGPU_CUDA_TRY(cudaLaunchKernel(func, dim3(grid), dim3(block), args, smem, stream));
+    }
+    return FPSGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// shared kernels
+// ---------------------------------------------------------------------------
+__global__ void transpose_to_soa(const float* __restrict__ pts, float* __restrict__ X, uint64_t n,
+                                 int dim) {
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n;
+         p += (uint64_t)gridDim.x * blockDim.x)
+        for (int d = 0; d < dim; ++d) X[(uint64_t)d * n + p] = pts[p * dim + d];
+}
+
+__global__ void compact_count(const uint8_t* flag, uint64_t n, uint32_t piece, uint32_t* bcount) {
+    const uint64_t lo = (uint64_t)blockIdx.x * kCompactChunk;
+    uint64_t hi = lo + kCompactChunk;
+    if (hi > n) hi = n;
+    uint32_t c = 0;
+    for (uint64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) c += run_start(flag, p, piece);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+    __shared__ uint32_t s[32];
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
+        bcount[blockIdx.x] = t;
+    }
+}
+
+// single block: exclusive scan of bcount in place, total to *total
+__global__ void compact_scan(uint32_t* bcount, uint32_t nblocks, uint32_t* total) {
+    __shared__ uint32_t s_w[64];
+    uint32_t carry = 0;
+    int par = 0;
+    for (uint32_t base = 0; base < nblocks; base += blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t v = i < nblocks ? bcount[i] : 0u;
+        // block exclusive scan of v (values may exceed 1: scan warp sums)
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t u = __shfl_up_sync(kFull, x, o);
+            if (lane >= o) x += u;
+        }
+        uint32_t* w = s_w + par * 32;
+        if (lane == 31) w[warp] = x;
+        __syncthreads();
+        const uint32_t c = lane < nwarps ? w[lane] : 0u;
+        uint32_t y = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t u = __shfl_up_sync(kFull, y, o);
+            if (lane >= o) y += u;
+        }
+        const uint32_t block_total = __shfl_sync(kFull, y, 31);
+        const uint32_t warp_excl = __shfl_sync(kFull, y - c, warp);
+        if (i < nblocks) bcount[i] = carry + warp_excl + (x - v);
+        carry += block_total;
+        par ^= 1;
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void compact_write(const uint8_t* flag, uint64_t n, uint32_t piece,
+                              const uint32_t* boff, const uint32_t* total, uint32_t* starts) {
+    __shared__ uint32_t s_w[64];
+    const uint64_t lo = (uint64_t)blockIdx.x * kCompactChunk;
+    uint64_t hi = lo + kCompactChunk;
+    if (hi > n) hi = n;
+    uint32_t running = boff[blockIdx.x];
+    int par = 0;
+    for (uint64_t base = lo; base < hi; base += blockDim.x) {
+        const uint64_t p = base + threadIdx.x;
+        const bool f = p < hi && run_start(flag, p, piece);
+        uint32_t tot;
+        const uint32_t r = block_rank(f, s_w, par, tot);
+        par ^= 1;
+        if (f) starts[running + r] = (uint32_t)p;
+        running += tot;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) starts[*total] = (uint32_t)n;
+}
+
+int kd_compact(const uint8_t* flag, uint64_t n, uint32_t piece, uint32_t* starts,
+               uint32_t* d_count, Scratch& sc, cudaStream_t stream) {
+    const uint64_t nblocks = (n + kCompactChunk - 1) / kCompactChunk;
+    uint32_t* bcount;
+    int rc;
+    if ((rc = sc.alloc(&bcount, nblocks))) return rc;
+    compact_count<<<(unsigned)nblocks, 1024, 0, stream>>>(flag, n, piece, bcount);
+    FPSGPU_CUDA_TRY(cudaGetLastError());
+    compact_scan<<<1, 1024, 0, stream>>>(bcount, (uint32_t)nblocks, d_count);
+    FPSGPU_CUDA_TRY(cudaGetLastError());
+    compact_write<<<(unsigned)nblocks, 1024, 0, stream>>>(flag, n, piece, bcount, d_count, starts);
+    FPSGPU_CUDA_TRY(cudaGetLastError());
+    return FPSGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// floating-point mode
+// ---------------------------------------------------------------------------
+namespace {
+std::once_flag g_mode_once;
+int g_fp_mode = FPSGPU_FP_NOFMA;
+std::mutex g_mode_mu;
+
+int fp_mode() {
+    std::call_once(g_mode_once, [] {
+        const char* e = std::getenv("FPSAMPLE_FP_MODE");
+        if (e && (std::strcmp(e, "fma") == 0 || std::strcmp(e, "FMA") == 0)) g_fp_mode = FPSGPU_FP_FMA;
+    });
+    std::lock_guard<std::mutex> lk(g_mode_mu);
+    return g_fp_mode;
+}
+}  // namespace
+
+}  // namespace fpsgpu
+
+using namespace fpsgpu;
+
+namespace {
+
+int resolve_stream(void* stream, DevCtx* ctx, cudaStream_t* out) {
+    int rc = current_ctx(ctx);
+    if (rc) return rc;
+    *out = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    return FPSGPU_OK;
+}
+
+int fps_device_impl(const float* d_points, size_t n, size_t dim, size_t k, const size_t* h_start,
+                    size_t n_start, uint64_t* d_out, float* d_trace, cudaStream_t stream, int sms) {
+    VanillaCall c{};
+    c.d_points = d_points;
+    c.n = n;
+    c.dim = (int)dim;
+    c.k = k;
+    c.h_starts = reinterpret_cast<const uint64_t*>(h_start);
+    c.n_starts = (uint32_t)n_start;
+    c.d_out = d_out;
+    c.d_trace = d_trace;
+    c.stream = stream;
+    c.sms = sms;
+    return fp_mode() == FPSGPU_FP_FMA ? run_vanilla_fma(c) : run_vanilla_nofma(c);
+}
+
+int check_fps_args(size_t n, size_t dim, size_t k, const size_t* start, size_t n_start) {
+    if (n == 0) return set_error(FPSGPU_ERR_ARG, "n_points must be >= 1");
+    if (dim == 0) return set_error(FPSGPU_ERR_DIM, "dim must be >= 1");
+    if (dim > 4096) return set_error(FPSGPU_ERR_DIM, "dim must be <= 4096, got %zu", dim);
+    if (n > 0xfffffffeull) return set_error(FPSGPU_ERR_ARG, "n_points must be < 2^32 - 1");
+    if (n_start == 0 || start == nullptr) return set_error(FPSGPU_ERR_ARG, "need at least one start index");
+    if (k > 0 && n_start > k)
+        return set_error(FPSGPU_ERR_ARG, "more start indices (%zu) than samples (%zu)", n_start, k);
+    if (n_start > 0xffffffffull) return set_error(FPSGPU_ERR_ARG, "too many start indices");
+    for (size_t i = 0; i < n_start; ++i)
+        if (start[i] >= n)
+            return set_error(FPSGPU_ERR_START, "start index %zu out of range (n_points=%zu)", start[i], n);
+    return FPSGPU_OK;
+}
+
+int check_kdline_args(size_t n, size_t dim, size_t start) {
+    if (dim == 0 || dim > 8) return set_error(FPSGPU_ERR_DIM, "dim must be in [1, 8], got %zu", dim);
+    if (start >= n) return set_error(FPSGPU_ERR_START, "start_idx %zu out of range (n_points=%zu)", start, n);
+    if (n > 0xfffffffeull) return set_error(FPSGPU_ERR_ARG, "n_points must be < 2^32 - 1");
+    return FPSGPU_OK;
+}
+
+int kdline_device_impl(const float* d_points, size_t n, size_t dim, size_t k, size_t start,
+                       size_t height, uint64_t* d_out, float* d_trace, cudaStream_t stream, int sms) {
+    KdlineCall c{};
+    c.d_points = d_points;
+    c.n = n;
+    c.dim = (int)dim;
+    c.k = k;
+    c.start = start;
+    c.height = height;
+    c.d_out = d_out;
+    c.d_trace = d_trace;
+    c.stream = stream;
+    c.sms = sms;
+    return fp_mode() == FPSGPU_FP_FMA ? run_kdline_fma(c) : run_kdline_nofma(c);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fpsgpu_last_error(void) { return t_last_error.c_str(); }
+
+const char* fpsgpu_version(void) { return FPSGPU_VERSION_STRING; }
+
+int fpsgpu_set_fp_mode(int mode) {
+    if (mode != FPSGPU_FP_NOFMA && mode != FPSGPU_FP_FMA)
+        return set_error(FPSGPU_ERR_ARG, "unknown fp mode %d", mode);
+    fp_mode();  // consume the environment default first
+    std::lock_guard<std::mutex> lk(g_mode_mu);
+    g_fp_mode = mode;
+    return FPSGPU_OK;
+}
+
+int fpsgpu_get_fp_mode(void) { return fp_mode(); }
+
+int fpsgpu_fps_device(const float* d_points, size_t n_points, size_t dim, size_t n_samples,
+                      const size_t* h_start, size_t n_start, uint64_t* d_out, float* d_trace,
+                      void* stream) {
+    clear_error();
+    int rc = check_fps_args(n_points, dim, n_samples, h_start, n_start);
+    if (rc) return rc;
+    if (n_samples == 0) return FPSGPU_OK;
+    DevCtx ctx;
+    cudaStream_t s;
+    if ((rc = resolve_stream(stream, &ctx, &s))) return rc;
+    return fps_device_impl(d_points, n_points, dim, n_samples, h_start, n_start, d_out, d_trace, s,
+                           ctx.sms);
+}
+
+int fpsgpu_fps(const float* raw_data, size_t n_points, size_t dim, size_t n_samples,
+               const size_t* start_idx, size_t n_start, size_t* sampled_point_indices) {
+    clear_error();
+    int rc = check_fps_args(n_points, dim, n_samples, start_idx, n_start);
+    if (rc) return rc;
+    if (n_samples == 0) return FPSGPU_OK;
+    DevCtx ctx;
+    if ((rc = current_ctx(&ctx))) return rc;
+    Scratch sc(ctx.stream);
+    float* d_pts;
+    uint64_t* d_out;
+    if ((rc = sc.alloc(&d_pts, n_points * dim))) return rc;
+    if ((rc = sc.alloc(&d_out, n_samples))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_pts, raw_data, n_points * dim * sizeof(float),
+                                    cudaMemcpyHostToDevice, ctx.stream));
+    if ((rc = fps_device_impl(d_pts, n_points, dim, n_samples, start_idx, n_start, d_out, nullptr,
+                              ctx.stream, ctx.sms)))
+        return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(sampled_point_indices, d_out, n_samples * sizeof(uint64_t),
+                                    cudaMemcpyDeviceToHost, ctx.stream));
+    FPSGPU_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
+    return FPSGPU_OK;
+}
+
+int fpsgpu_kdline_device(const float* d_points, size_t n_points, size_t dim, size_t n_samples,
+                         size_t start_idx, size_t height, uint64_t* d_out, float* d_trace,
+                         void* stream) {
+    clear_error();
+    int rc = check_kdline_args(n_points, dim, start_idx);
+    if (rc) return rc;
+    if (n_samples == 0) return FPSGPU_OK;
+    DevCtx ctx;
+    cudaStream_t s;
+    if ((rc = resolve_stream(stream, &ctx, &s))) return rc;
+    return kdline_device_impl(d_points, n_points, dim, n_samples, start_idx, height, d_out, d_trace,
+                              s, ctx.sms);
+}
+
+int bucket_fps_kdline(const float* raw_data, size_t n_points, size_t dim, size_t n_samples,
+                      size_t start_idx, size_t height, size_t* sampled_point_indices) {
+    clear_error();
+    int rc = check_kdline_args(n_points, dim, start_idx);
+    if (rc) return rc;
+    if (n_samples == 0) return FPSGPU_OK;
+    DevCtx ctx;
+    if ((rc = current_ctx(&ctx))) return rc;
+    Scratch sc(ctx.stream);
+    float* d_pts;
+    uint64_t* d_out;
+    if ((rc = sc.alloc(&d_pts, n_points * dim))) return rc;
+    if ((rc = sc.alloc(&d_out, n_samples))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_pts, raw_data, n_points * dim * sizeof(float),
+                                    cudaMemcpyHostToDevice, ctx.stream));
+    if ((rc = kdline_device_impl(d_pts, n_points, dim, n_samples, start_idx, height, d_out, nullptr,
+                                 ctx.stream, ctx.sms)))
+        return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(sampled_point_indices, d_out, n_samples * sizeof(uint64_t),
+                                    cudaMemcpyDeviceToHost, ctx.stream));
+    FPSGPU_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
+    return FPSGPU_OK;
+}
+
+int fpsgpu_kdline_build(const float* raw_data, size_t n_points, size_t dim, size_t height,
+                        uint64_t* h_perm, uint64_t* h_bucket_start, size_t* n_buckets) {
+    clear_error();
+    int rc = check_kdline_args(n_points, dim, 0);
+    if (rc) return rc;
+    if (!h_perm || !h_bucket_start || !n_buckets) return set_error(FPSGPU_ERR_ARG, "null output");
+    DevCtx ctx;
+    if ((rc = current_ctx(&ctx))) return rc;
+    Scratch sc(ctx.stream);
+    float* d_pts;
+    if ((rc = sc.alloc(&d_pts, n_points * dim))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_pts, raw_data, n_points * dim * sizeof(float),
+                                    cudaMemcpyHostToDevice, ctx.stream));
+    KdlineCall c{};
+    c.d_points = d_pts;
+    c.n = n_points;
+    c.dim = (int)dim;
+    c.height = height;
+    c.stream = ctx.stream;
+    c.sms = ctx.sms;
+    c.h_perm = h_perm;
+    c.h_bucket_start = h_bucket_start;
+    c.h_n_buckets = n_buckets;
+    return fp_mode() == FPSGPU_FP_FMA ? run_kdline_fma(c) : run_kdline_nofma(c);
+}
+
+}  // extern "C"

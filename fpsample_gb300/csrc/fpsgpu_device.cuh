@@ -1,0 +1,163 @@
+// Device-side building blocks shared by the FPS kernels (sm_103a).
+//
+// * sqdist<D,FMA>: the reference's fp32 squared distance, bit for bit.
+//   Reference: src/lib.cpp:214-221 (vanilla) and src/_ext/Point.h:48-53 with
+//   utils.h:12-16 (kd-line).  Both sum (p_j - r_j)^2 over j = 0..D-1 in order.
+//   FMA=false rounds every operation ((d0*d0 + d1*d1) + d2*d2); FMA=true is the
+//   contracted chain fma(d2,d2,fma(d1,d1,d0*d0)) that a contracting host
+//   compiler produces.  The explicit __f*_rn intrinsics stop nvcc from
+//   contracting on its own.
+// * 64-bit argmax keys: (valid bit 63) | (distance bits << 32) | tie field.
+//   Distances are never negative or NaN, so their IEEE bits order like their
+//   values.  The tie field is the position itself where the HIGHEST index wins
+//   (vanilla, lib.cpp:226 uses >=) and its complement where the LOWEST position
+//   wins (kd-line, KDNode.h:97,155 and KDLineTree.h:61 use strict >).
+// * warp/block argmax via redux.sync, and the cross-CTA all-gather exchange
+//   used by the persistent multi-CTA kernels.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fpsgpu {
+
+constexpr uint64_t kKeyValid = 1ull << 63;
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kMaxDim = 8;
+
+// error word bits (device -> host)
+constexpr int kErrExchangeTimeout = 1;
+constexpr int kErrNonFiniteSplit = 2;
+constexpr int kErrBadIndex = 4;
+
+// Upper bound on polls of one exchange slot before a CTA gives up, sets the
+// error word and leaves the kernel (each poll is one L2 round trip, so this is
+// a few seconds).
+constexpr long long kSpinLimit = 1ll << 23;
+
+template <int D, bool FMA>
+__device__ __forceinline__ float sqdist(const float* p, const float* r) {
+    float d = __fsub_rn(p[0], r[0]);
+    float acc = __fmul_rn(d, d);
+#pragma unroll
+    for (int j = 1; j < D; ++j) {
+        float e = __fsub_rn(p[j], r[j]);
+        acc = FMA ? __fmaf_rn(e, e, acc) : __fadd_rn(acc, __fmul_rn(e, e));
+    }
+    return acc;
+}
+
+// Runtime-dimension variant (same operation order), for D > 8 in vanilla FPS.
+template <bool FMA>
+__device__ __forceinline__ float sqdist_rt(const float* __restrict__ X, uint64_t stride, uint64_t p,
+                                           const float* r, int dim) {
+    float d = __fsub_rn(X[p], r[0]);
+    float acc = __fmul_rn(d, d);
+    for (int j = 1; j < dim; ++j) {
+        float e = __fsub_rn(X[(uint64_t)j * stride + p], r[j]);
+        acc = FMA ? __fmaf_rn(e, e, acc) : __fadd_rn(acc, __fmul_rn(e, e));
+    }
+    return acc;
+}
+
+// Squared gap from r to the box [lo, hi], with the same operation structure as
+// sqdist.  Rounding is monotone, so for every point p inside the box
+// bound <= sqdist(p, r) in the same mode: a box whose bound is >= the largest
+// running distance inside it cannot have any distance lowered by r.
+template <int D, bool FMA>
+__device__ __forceinline__ float box_bound(const float* lo, const float* hi, const float* r) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+        float g = 0.0f;
+        if (r[j] > hi[j]) g = __fsub_rn(r[j], hi[j]);
+        else if (r[j] < lo[j]) g = __fsub_rn(lo[j], r[j]);
+        if (j == 0) acc = __fmul_rn(g, g);
+        else acc = FMA ? __fmaf_rn(g, g, acc) : __fadd_rn(acc, __fmul_rn(g, g));
+    }
+    return acc;
+}
+
+__device__ __forceinline__ uint64_t key_high_wins(float dist, uint32_t pos) {
+    return kKeyValid | ((uint64_t)__float_as_uint(dist) << 32) | pos;
+}
+__device__ __forceinline__ uint64_t key_low_wins(float dist, uint32_t pos) {
+    return kKeyValid | ((uint64_t)__float_as_uint(dist) << 32) | (0xffffffffu - pos);
+}
+__device__ __forceinline__ float key_dist(uint64_t key) {
+    return __uint_as_float((uint32_t)(key >> 32) & 0x7fffffffu);
+}
+template <bool LOW_WINS>
+__device__ __forceinline__ uint32_t key_pos(uint64_t key) {
+    uint32_t t = (uint32_t)key;
+    return LOW_WINS ? 0xffffffffu - t : t;
+}
+
+// Max of a 64-bit key over the full warp: two redux.sync steps.
+__device__ __forceinline__ uint64_t warp_max_key(uint64_t k) {
+    uint32_t hi = (uint32_t)(k >> 32), lo = (uint32_t)k;
+    uint32_t mh = __reduce_max_sync(kFull, hi);
+    uint32_t ml = __reduce_max_sync(kFull, hi == mh ? lo : 0u);
+    return ((uint64_t)mh << 32) | ml;
+}
+
+__device__ __forceinline__ void st_release_gpu(uint64_t* p, uint64_t v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed_gpu(uint64_t* p, uint64_t v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t ld_acquire_gpu(const uint64_t* p) {
+    uint64_t v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_relaxed_gpu_s32(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Cross-CTA argmax for persistent kernels whose CTAs are all co-resident
+// (cooperative launch).  Called by ONE full warp per CTA, once per round.
+//
+// slots: 3 * G u64, zeroed before the launch.  Round t uses row t % 3.  Every
+// CTA publishes its key (never 0: bit 63 is set) with a release store, then
+// polls the whole row with acquire loads until every entry is non-zero.  When
+// a CTA has seen all of round t, every CTA has finished reading round t-1, so
+// it clears its own round-(t-1) entry, which it will not publish into again
+// before round t+2; the clear is ordered before its round t+1 release store,
+// so a reader of round t+2 can never see the stale value.
+//
+// A CTA without candidates publishes kKeyValid alone, which never beats a
+// real key of a valid point.  Returns 0 (and sets err) if a slot stays empty
+// for kSpinLimit polls.
+__device__ __forceinline__ uint64_t exchange_max(uint64_t* slots, int G, uint32_t round,
+                                                 uint64_t my_key, int* err) {
+    const int lane = threadIdx.x & 31;
+    uint64_t* row = slots + (uint64_t)(round % 3u) * G;
+    if (lane == 0) st_release_gpu(row + blockIdx.x, my_key | kKeyValid);
+    uint64_t best = 0;
+    bool ok = true;
+    for (int j = lane; j < G; j += 32) {
+        uint64_t v = 0;
+        long long spins = 0;
+        while ((v = ld_acquire_gpu(row + j)) == 0ull) {
+            if (++spins > kSpinLimit) {
+                ok = false;
+                break;
+            }
+        }
+        best = v > best ? v : best;
+    }
+    if (__any_sync(kFull, !ok)) {
+        if (lane == 0) atomicOr(err, kErrExchangeTimeout);
+        return 0;
+    }
+    best = warp_max_key(best);
+    if (lane == 0) st_relaxed_gpu(slots + (uint64_t)((round + 2u) % 3u) * G + blockIdx.x, 0ull);
+    return best;
+}
+
+}  // namespace fpsgpu

@@ -1,0 +1,102 @@
+// Host-side internals shared by the translation units of libfpsgpu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+#include "../../include/fpsgpu.h"
+
+namespace fpsgpu {
+
+// Records a message for fpsgpu_last_error() on this thread and returns code.
+int set_error(int code, const char* fmt, ...);
+void clear_error();
+
+#define FPSGPU_CUDA_TRY(expr)                                                              \
+    do {                                                                                   \
+        cudaError_t e_ = (expr);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return ::fpsgpu::set_error(FPSGPU_ERR_CUDA, "%s failed: %s (%s:%d)", #expr,    \
+                                       cudaGetErrorString(e_), __FILE__, __LINE__);        \
+    } while (0)
+
+// Properties of the current device plus the library's own stream on it.
+struct DevCtx {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+};
+int current_ctx(DevCtx* ctx);
+
+// Stream-ordered scratch: every allocation is released with cudaFreeAsync on
+// the same stream when the object goes out of scope.
+class Scratch {
+   public:
+    explicit Scratch(cudaStream_t s) : s_(s) {}
+    ~Scratch() {
+        for (void* p : ptrs_) cudaFreeAsync(p, s_);
+    }
+    Scratch(const Scratch&) = delete;
+    Scratch& operator=(const Scratch&) = delete;
+    template <class T>
+    int alloc(T** out, size_t count) {
+        void* p = nullptr;
+        size_t bytes = count ? count * sizeof(T) : sizeof(T);
+        cudaError_t e = cudaMallocAsync(&p, bytes, s_);
+        if (e != cudaSuccess)
+            return set_error(FPSGPU_ERR_CUDA, "cudaMallocAsync(%zu bytes) failed: %s", bytes,
+                             cudaGetErrorString(e));
+        ptrs_.push_back(p);
+        *out = static_cast<T*>(p);
+        return FPSGPU_OK;
+    }
+
+   private:
+    cudaStream_t s_;
+    std::vector<void*> ptrs_;
+};
+
+// One vanilla FPS call on device buffers.
+struct VanillaCall {
+    const float* d_points;  // row-major [n][dim]
+    uint64_t n;
+    int dim;
+    uint64_t k;
+    const uint64_t* h_starts;
+    uint32_t n_starts;
+    uint64_t* d_out;
+    float* d_trace;
+    cudaStream_t stream;
+    int sms;
+};
+int run_vanilla_nofma(const VanillaCall& c);
+int run_vanilla_fma(const VanillaCall& c);
+
+// One kd-line QuickFPS call on device buffers.
+struct KdlineCall {
+    const float* d_points;  // row-major [n][dim]
+    uint64_t n;
+    int dim;
+    uint64_t k;
+    uint64_t start;
+    uint64_t height;
+    uint64_t* d_out;
+    float* d_trace;
+    cudaStream_t stream;
+    int sms;
+    // build-only mode (k ignored): host outputs
+    uint64_t* h_perm;
+    uint64_t* h_bucket_start;
+    size_t* h_n_buckets;
+};
+int run_kdline_nofma(const KdlineCall& c);
+int run_kdline_fma(const KdlineCall& c);
+
+// cooperative launch helper: refuses grids that cannot be co-resident
+int launch_persistent(const void* func, int grid, int block, void** args, size_t smem,
+                      cudaStream_t stream, bool cooperative);
+
+}  // namespace fpsgpu

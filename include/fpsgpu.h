@@ -1,0 +1,112 @@
+/*
+ * fpsgpu.h -- C ABI of libfpsgpu, the GB300 (sm_103a) farthest-point-sampling
+ * library behind fpsample_gb300.
+ *
+ * Conventions (all entry points):
+ *   - plain pointers and sizes only; the caller owns every buffer;
+ *   - points are row-major float32 [n_points][dim];
+ *   - sampled indices are uint64 (size_t on LP64 hosts), original point ids;
+ *   - return 0 on success, a positive FPSGPU_ERR_* code otherwise, with a
+ *     message for the calling thread in fpsgpu_last_error();
+ *   - every call runs on the CUDA device that is current on the calling thread;
+ *   - there is no CPU fallback: without a usable GPU the calls fail with
+ *     FPSGPU_ERR_CUDA.
+ *
+ * Floating point: distances are computed exactly as the reference computes
+ * them (fp32, dimensions summed in order).  Whether a*b+c is fused into an FMA
+ * changes results, so the library has two modes (fpsgpu_set_fp_mode): the
+ * default FPSGPU_FP_NOFMA matches a reference build that does not contract
+ * (the default x86-64 build); FPSGPU_FP_FMA matches a contracting build (GCC's
+ * default on aarch64, or x86-64 with -mfma).
+ */
+#ifndef FPSGPU_H
+#define FPSGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* error codes; 1 and 2 are the reference's own (src/wrapper.hpp:105-111,121-127) */
+#define FPSGPU_OK 0
+#define FPSGPU_ERR_DIM 1          /* dim outside the supported range            */
+#define FPSGPU_ERR_START 2        /* a start index >= n_points                  */
+#define FPSGPU_ERR_ARG 3          /* any other invalid argument                 */
+#define FPSGPU_ERR_CUDA 4         /* CUDA runtime error (no device, OOM, ...)   */
+#define FPSGPU_ERR_DEVICE 5       /* a kernel gave up waiting (bounded spin)    */
+#define FPSGPU_ERR_NONFINITE 6    /* NaN met by the kd-line build's partition   */
+
+#define FPSGPU_FP_NOFMA 0
+#define FPSGPU_FP_FMA 1
+
+/*
+ * Replaces the reference's C ABI of the same name and signature
+ * (src/wrapper.hpp:118-132): QuickFPS with a kd-line bucket tree of `height`.
+ * The first sample is the point at position start_idx of the tree build's
+ * permuted order, exactly as the reference (wrapper.hpp:54-55).
+ * Host buffers in and out; synchronous.  dim must be in [1, 8] (returns 1),
+ * start_idx < n_points (returns 2).
+ */
+int bucket_fps_kdline(const float *raw_data, size_t n_points, size_t dim,
+                      size_t n_samples, size_t start_idx, size_t height,
+                      size_t *sampled_point_indices);
+
+/*
+ * Vanilla FPS with one or more start indices.  The reference has no C ABI for
+ * this path; this is the C form of _fps_sampling (src/lib.cpp:249-270), which
+ * dispatches to fps_sampling (lib.cpp:188-246, n_start == 1) and
+ * fps_sampling_multi_start_index (lib.cpp:111-186).  The first n_start outputs
+ * are the given starts; later ties go to the highest index.
+ * Host buffers; synchronous.  Any dim >= 1.
+ */
+int fpsgpu_fps(const float *raw_data, size_t n_points, size_t dim,
+               size_t n_samples, const size_t *start_idx, size_t n_start,
+               size_t *sampled_point_indices);
+
+/*
+ * Device-buffer forms of the two calls above (same semantics as
+ * bucket_fps_kdline / fpsgpu_fps).  d_points and d_out (n_samples uint64) are
+ * device pointers; d_trace is NULL or n_samples floats receiving the running
+ * min-distance of every chosen point when it was chosen (the max-min trace;
+ * FLT_MAX / +inf for the first and forced samples).  h_start is a HOST array.
+ * stream is a cudaStream_t (NULL: the library's own stream).  The call
+ * returns when the result is in d_out.
+ */
+int fpsgpu_kdline_device(const float *d_points, size_t n_points, size_t dim,
+                         size_t n_samples, size_t start_idx, size_t height,
+                         uint64_t *d_out, float *d_trace, void *stream);
+
+int fpsgpu_fps_device(const float *d_points, size_t n_points, size_t dim,
+                      size_t n_samples, const size_t *h_start, size_t n_start,
+                      uint64_t *d_out, float *d_trace, void *stream);
+
+/*
+ * The kd-line tree build alone (KDTreeBase.h:84-207 of the reference), for
+ * inspection and tests: h_perm (n_points, HOST) receives the original index of
+ * the point at every position of the permuted order, h_bucket_start (HOST,
+ * capacity n_points) the first position of every bucket in order, and
+ * *n_buckets their number.
+ */
+int fpsgpu_kdline_build(const float *raw_data, size_t n_points, size_t dim,
+                        size_t height, uint64_t *h_perm, uint64_t *h_bucket_start,
+                        size_t *n_buckets);
+
+/* floating-point mode for subsequent calls from any thread (FPSGPU_FP_*).
+   Initial value: environment variable FPSAMPLE_FP_MODE ("fma" / "nofma"),
+   else FPSGPU_FP_NOFMA. */
+int fpsgpu_set_fp_mode(int mode);
+int fpsgpu_get_fp_mode(void);
+
+/* message describing the last failure on the calling thread ("" if none) */
+const char *fpsgpu_last_error(void);
+
+/* library version string */
+const char *fpsgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FPSGPU_H */

@@ -1,0 +1,91 @@
+"""CPU: the drop-in Python API validates arguments exactly like the reference
+(src/fpsample/__init__.py and src/lib.cpp) before any GPU work, and without a
+GPU every sampling call fails loudly instead of falling back to the CPU."""
+import numpy as np
+import pytest
+
+import fpsample_gb300 as fps
+from fpsample_gb300 import _fpsample
+
+PC = np.random.default_rng(0).random((64, 3))
+
+
+@pytest.mark.parametrize(
+    "call,exc",
+    [
+        (lambda: fps.fps_sampling(PC, 0, 0), AssertionError),
+        (lambda: fps.fps_sampling(PC[0], 4, 0), AssertionError),
+        (lambda: fps.fps_sampling(PC, 65, 0), AssertionError),
+        (lambda: fps.fps_sampling(PC, 4, 64), AssertionError),
+        (lambda: fps.fps_sampling(PC, 4, -1), AssertionError),
+        (lambda: fps.fps_sampling(PC, 2, [0, 1, 2]), AssertionError),
+        (lambda: fps.fps_sampling(PC, 4, [0, 64]), AssertionError),
+        (lambda: fps.fps_sampling(PC, 4, np.int64(3)), ValueError),
+        (lambda: fps.fps_sampling(PC, 4, (1, 2)), ValueError),
+        (lambda: fps.bucket_fps_kdline_sampling(PC, 0, 3, 0), AssertionError),
+        (lambda: fps.bucket_fps_kdline_sampling(PC, 4, 0, 0), AssertionError),
+        (lambda: fps.bucket_fps_kdline_sampling(PC, 4, 7, 0), AssertionError),
+        (lambda: fps.bucket_fps_kdline_sampling(PC, 4, 3, 64), AssertionError),
+        (lambda: fps.bucket_fps_kdline_sampling(PC, 4, 3, [0, 1]), TypeError),
+        (lambda: fps.bucket_fps_kdline_sampling(PC, 65, 3, 0), AssertionError),
+    ],
+)
+def test_python_wrapper_errors(call, exc):
+    with pytest.raises(exc):
+        call()
+
+
+def test_extension_errors_match_reference():
+    pc = np.zeros((10, 3), np.float32)
+    with pytest.raises(TypeError, match="start_idx must be int or 1D numpy array of size_t"):
+        _fpsample._fps_sampling(pc, 3, 1.5)
+    with pytest.raises(TypeError):
+        _fpsample._fps_sampling(pc, 3, np.array([1], np.int64))
+    with pytest.raises(ValueError, match="points must be a 2D array"):
+        _fpsample._fps_sampling(np.zeros(10, np.float32), 3, 0)
+    with pytest.raises(ValueError, match="at least one column"):
+        _fpsample._fps_sampling(np.zeros((10, 0), np.float32), 3, 0)
+    with pytest.raises(ValueError, match="n_samples must be less than the number of points"):
+        _fpsample._fps_sampling(pc, 11, 0)
+    with pytest.raises(ValueError, match="start_idx must be less than the number of points"):
+        _fpsample._fps_sampling(pc, 3, 10)
+    with pytest.raises(ValueError, match="The number of start indices"):
+        _fpsample._fps_sampling(pc, 1, np.array([1, 2], np.uint64))
+    with pytest.raises(ValueError, match="All indices in start_idx"):
+        _fpsample._fps_sampling(pc, 3, np.array([1, 10], np.uint64))
+    with pytest.raises(NotImplementedError, match="Array of start indices not implemented yet"):
+        _fpsample._bucket_fps_kdline_sampling(pc, 3, 2, np.array([1], np.uint64))
+    with pytest.raises(ValueError, match="points must be a 2D float32 array"):
+        _fpsample._bucket_fps_kdline_sampling(np.zeros(10, np.float32), 3, 2, 0)
+    with pytest.raises(ValueError, match="start_idx out of range"):
+        _fpsample._bucket_fps_kdline_sampling(pc, 3, 2, 10)
+    with pytest.raises(ValueError, match=r"n_samples must be in \[1, num_points\]"):
+        _fpsample._bucket_fps_kdline_sampling(pc, 0, 2, 0)
+    with pytest.raises(ValueError, match="height must be >= 1"):
+        _fpsample._bucket_fps_kdline_sampling(pc, 3, 0, 0)
+    # C-ABI error codes surface as RuntimeError with the reference's message
+    with pytest.raises(RuntimeError, match="bucket_fps_kdline failed with error code 1"):
+        _fpsample._bucket_fps_kdline_sampling(np.zeros((10, 9), np.float32), 3, 2, 0)
+
+
+def test_out_of_scope_variants_raise():
+    for f in (lambda: fps.fps_npdu_sampling(PC, 4), lambda: fps.fps_npdu_kdtree_sampling(PC, 4),
+              lambda: fps.bucket_fps_kdtree_sampling(PC, 4)):
+        with pytest.raises(NotImplementedError):
+            f()
+
+
+def test_exports_and_version():
+    for name in ("fps_sampling", "bucket_fps_kdline_sampling", "fps_npdu_sampling",
+                 "fps_npdu_kdtree_sampling", "bucket_fps_kdtree_sampling", "__version__"):
+        assert hasattr(fps, name)
+    assert fps.__version__.startswith("1.0.2")
+
+
+def test_random_start_uses_numpy_global_state():
+    np.random.seed(123)
+    a = fps.get_start_idx(1000, None)
+    np.random.seed(123)
+    assert a == np.random.randint(low=0, high=1000)
+    assert isinstance(fps.get_start_idx(10, [1, 2]), np.ndarray)
+    assert fps.get_start_idx(10, [1, 2]).dtype == np.uint64

@@ -1,0 +1,177 @@
+"""GPU parity: every result must equal the reference's, bit for bit.
+
+Sources of truth, in order:
+  1. golden vectors produced by the unmodified reference (tests/golden/);
+  2. the oracle (oracle/fps_oracle.c, itself pinned to 1.) on seeded inputs;
+  3. at full workload sizes, where the oracle is too slow, oracle prefixes plus
+     size-independent FPS properties (non-increasing max-min trace, fp64 trace).
+Indices are compared exactly; the fp32 trace against an fp64 recomputation
+within rtol 1e-5.
+"""
+import numpy as np
+import pytest
+
+import fpsample_gb300 as fps
+from fpsample_gb300 import capi
+from fpsample_gb300 import workloads as W
+from oracle.oracle import Oracle, fp64_trace
+from tests.golden.golden import load_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = load_cases()
+ORACLE = Oracle()
+MODES = ["nofma", "fma"]
+
+
+@pytest.fixture(params=MODES)
+def mode(request):
+    fps.set_fp_mode(request.param)
+    yield request.param
+    fps.set_fp_mode("nofma")
+
+
+def _api(case):
+    pts = case["points"]
+    if case["op"] == "fps":
+        st = case["start"]
+        return fps.fps_sampling(pts, case["k"], st)
+    return fps.bucket_fps_kdline_sampling(pts, case["k"], case["h"], case["start"])
+
+
+def _cabi(case):
+    pts = case["points"]
+    if case["op"] == "fps":
+        return capi.fps(pts, case["k"], case["start"])
+    return capi.bucket_fps_kdline(pts, case["k"], case["start"], case["h"])
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_golden_python_api(case, mode):
+    got = _api(case)
+    assert got.dtype == np.uint64
+    np.testing.assert_array_equal(got, case["expected"][mode])
+
+
+@pytest.mark.parametrize("case", CASES[::3], ids=[c["name"] for c in CASES[::3]])
+def test_golden_c_abi(case, mode):
+    np.testing.assert_array_equal(_cabi(case), case["expected"][mode])
+
+
+def _random_case(seed):
+    rng = np.random.default_rng(1000 + seed)
+    n = int(rng.integers(2, 20000))
+    d = int(rng.integers(1, 9))
+    kind = seed % 3
+    if kind == 0:
+        pts = rng.random((n, d)).astype(np.float32)
+    elif kind == 1:
+        pts = rng.integers(0, 5, (n, d)).astype(np.float32)
+    else:
+        pts = (rng.standard_normal((n, d)) * rng.uniform(0.01, 100)).astype(np.float32)
+    k = int(rng.integers(1, min(n, 3000) + 1))
+    s = int(rng.integers(0, n))
+    h = int(rng.integers(1, max(2, int(np.log2(n)) + 1)))
+    return pts, k, s, h
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_vs_oracle(seed, mode):
+    pts, k, s, h = _random_case(seed)
+    np.testing.assert_array_equal(fps.fps_sampling(pts, k, s), ORACLE.fps(pts, k, s, mode))
+    np.testing.assert_array_equal(fps.bucket_fps_kdline_sampling(pts, k, h, s),
+                                  ORACLE.kdline(pts, k, h, s, mode))
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_multi_start_vs_oracle(seed, mode):
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(100, 30000))
+    pts = rng.random((n, 3)).astype(np.float32)
+    m = int(rng.integers(1, 8))
+    starts = [int(x) for x in rng.integers(0, n, m)]
+    if seed == 0:
+        starts = [5, 5, 5]  # duplicated starts are allowed
+    k = int(rng.integers(m, min(n, 2000) + 1))
+    np.testing.assert_array_equal(fps.fps_sampling(pts, k, starts), ORACLE.fps(pts, k, starts, mode))
+
+
+@pytest.mark.parametrize("h", [0, 1, 3, 7, 11, 40])
+def test_build_permutation_vs_oracle(h):
+    rng = np.random.default_rng(h)
+    for pts in (rng.random((3000, 3)).astype(np.float32),
+                rng.integers(0, 3, (2000, 2)).astype(np.float32),
+                np.full((300, 4), 1.5, np.float32)):
+        perm, bst = capi.kdline_build(pts, h)
+        operm, obst = ORACLE.kdline_build(pts, h)
+        np.testing.assert_array_equal(perm, operm)
+        np.testing.assert_array_equal(bst, obst)
+
+
+@pytest.mark.parametrize("n,h", [(100, 40), (37, 64), (5, 3), (1, 5), (1000, 0)])
+def test_c_abi_heights_beyond_the_python_check(n, h, mode):
+    # the C ABI accepts any height (the Python wrapper asserts 2**h <= n)
+    pts = np.random.default_rng(n).random((n, 3)).astype(np.float32)
+    k = min(n, 50)
+    np.testing.assert_array_equal(capi.bucket_fps_kdline(pts, k, n // 2, h),
+                                  ORACLE.kdline(pts, k, h, n // 2, mode))
+
+
+def test_more_samples_than_points_c_abi(mode):
+    pts = np.random.default_rng(9).random((40, 3)).astype(np.float32)
+    np.testing.assert_array_equal(capi.bucket_fps_kdline(pts, 100, 3, 2), ORACLE.kdline(pts, 100, 2, 3, mode))
+    np.testing.assert_array_equal(capi.fps(pts, 100, 3), ORACLE.fps(pts, 100, 3, mode))
+
+
+def test_high_dimension_vanilla(mode):
+    rng = np.random.default_rng(5)
+    for d in (9, 16, 33):
+        pts = rng.random((3000, d)).astype(np.float32)
+        np.testing.assert_array_equal(fps.fps_sampling(pts, 300, 1), ORACLE.fps(pts, 300, 1, mode))
+
+
+def test_nan_coordinates_vanilla_exact():
+    pts = np.random.default_rng(6).random((500, 3)).astype(np.float32)
+    pts[[3, 77, 400], 1] = np.nan
+    np.testing.assert_array_equal(fps.fps_sampling(pts, 100, 0), ORACLE.fps(pts, 100, 0))
+
+
+def test_kdline_nan_in_split_dimension_is_reported():
+    pts = np.random.default_rng(6).random((500, 3)).astype(np.float32)
+    pts[3, :] = np.nan
+    with pytest.raises(RuntimeError, match="error code 6"):
+        fps.bucket_fps_kdline_sampling(pts, 10, 3, 0)
+
+
+def test_device_tensor_entry_points():
+    torch = pytest.importorskip("torch")
+    pts = W.gmm_cloud(200_000, seed=7)
+    t = torch.from_numpy(pts).cuda()
+    out, tr = capi.kdline_tensor(t, 2000, 7, 0, trace=True)
+    np.testing.assert_array_equal(out.cpu().numpy().astype(np.uint64), ORACLE.kdline(pts, 2000, 7, 0))
+    out2, tr2 = capi.fps_tensor(t, 2000, [0, 9], trace=True)
+    np.testing.assert_array_equal(out2.cpu().numpy().astype(np.uint64), ORACLE.fps(pts, 2000, [0, 9]))
+    ref = fp64_trace(pts, out2.cpu().numpy())
+    np.testing.assert_allclose(tr2.cpu().numpy()[2:], ref[2:], rtol=1e-5)
+    t1 = tr.cpu().numpy()
+    assert np.all(np.diff(t1[1:]) <= 0)  # FPS max-min trace never increases
+
+
+def test_gmm_1m_kdline_h7_full(mode):
+    """gmm-1m workload at full size: N=1,048,576, h=7, K=16,384."""
+    pts = W.gmm_cloud(1 << 20, seed=W.SEEDS["gmm-1m"])
+    got = fps.bucket_fps_kdline_sampling(pts, 16384, 7, 0)
+    np.testing.assert_array_equal(got, ORACLE.kdline(pts, 16384, 7, 0, mode))
+
+
+def test_gmm_1m_vanilla_prefix():
+    """Vanilla FPS on the same 1M cloud: full K on the GPU; the oracle checks a
+    prefix (FPS is prefix-stable in K) and the whole trace is non-increasing."""
+    torch = pytest.importorskip("torch")
+    pts = W.gmm_cloud(1 << 20, seed=W.SEEDS["gmm-1m"])
+    out, tr = capi.fps_tensor(torch.from_numpy(pts).cuda(), 16384, 0, trace=True)
+    out = out.cpu().numpy().astype(np.uint64)
+    np.testing.assert_array_equal(out[:256], ORACLE.fps(pts, 256, 0))
+    t = tr.cpu().numpy()
+    assert np.all(np.diff(t[1:]) <= 0)
+    assert len(np.unique(out)) == 16384

@@ -1,0 +1,69 @@
+"""CPU: the oracle (C restatement of the reference) against the golden vectors
+produced by the unmodified reference, and internal consistency checks."""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle, fp64_trace
+from tests.golden.golden import load_cases
+
+CASES = load_cases()
+ORACLE = Oracle()
+
+
+def test_golden_inputs_regenerate():
+    bad = [c["name"] for c in CASES if not c["input_ok"]]
+    assert not bad, f"regenerated inputs differ from the ones the reference saw: {bad}"
+
+
+@pytest.mark.parametrize("mode", ["nofma", "fma"])
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_oracle_matches_reference(case, mode):
+    pts = case["points"]
+    if case["op"] == "fps":
+        got = ORACLE.fps(pts, case["k"], case["start"], mode)
+    else:
+        got = ORACLE.kdline(pts, case["k"], case["h"], case["start"], mode)
+    np.testing.assert_array_equal(got, case["expected"][mode])
+
+
+def test_fma_builds_really_differ():
+    # the golden set contains a case where the two reference builds disagree,
+    # so the mode switch is exercised for real
+    c = next(c for c in CASES if c["name"] == "gmm128k_kdline_h7")
+    d = np.nonzero(c["expected"]["nofma"] != c["expected"]["fma"])[0]
+    assert d.size > 0 and d[0] == 3912
+
+
+@pytest.mark.parametrize("seed", range(6))
+@pytest.mark.parametrize("mode", ["nofma", "fma"])
+def test_kdline_equals_fps_over_permuted_order(seed, mode):
+    """The bucket pruning never changes a value: kd-line output equals plain FPS
+    over the build's permuted order with first-position ties."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(50, 3000))
+    d = int(rng.integers(1, 9))
+    pts = rng.random((n, d)).astype(np.float32)
+    if seed % 2:
+        pts = np.round(pts * 3) / 3  # ties
+    h = int(rng.integers(1, 8))
+    k = int(rng.integers(1, n + 1))
+    s = int(rng.integers(0, n))
+    a = ORACLE.kdline(pts, k, h, s, mode)
+    b = ORACLE.kdline_direct(pts, k, h, s, mode)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_build_permutation_is_a_permutation_and_buckets_ordered():
+    rng = np.random.default_rng(3)
+    pts = rng.random((5000, 3)).astype(np.float32)
+    perm, bst = ORACLE.kdline_build(pts, 6)
+    assert np.array_equal(np.sort(perm), np.arange(5000))
+    assert bst[0] == 0 and np.all(np.diff(bst.astype(np.int64)) > 0) and len(bst) == 64
+
+
+def test_fp64_trace_close_to_fp32():
+    rng = np.random.default_rng(4)
+    pts = rng.random((2000, 3)).astype(np.float32)
+    idx, tr = ORACLE.fps(pts, 200, 0, "nofma", trace=True)
+    ref = fp64_trace(pts, idx)
+    np.testing.assert_allclose(tr[1:], ref[1:], rtol=1e-5)
