@@ -240,7 +240,8 @@ template <int D, bool FMA, int PPT>
 int launch_resident(const VanillaCall& c, VanillaArgs a, int G) {
     auto kern = vanilla_resident<D, FMA, PPT>;
     size_t smem = a.smem_cloud ? (size_t)c.n * D * sizeof(float) : 0;
-    if (smem > 48 * 1024)
+    // static + dynamic shared memory above 48 KB needs the opt-in attribute
+    if (smem > 0)
         FPSGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem));
     void* args[] = {&a};
@@ -319,7 +320,7 @@ int run_vanilla_d(const VanillaCall& c) {
         a.slots = slots;
         auto kern = vanilla_stream<D, FMA>;
         size_t smem = D > 0 ? 0 : (size_t)c.dim * sizeof(float);
-        if (smem > 48 * 1024)
+        if (smem > 0)
             FPSGPU_CUDA_TRY(cudaFuncSetAttribute(
                 kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         void* args[] = {&a};
