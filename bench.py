@@ -1,0 +1,401 @@
+#!/usr/bin/env python
+"""Benchmark of the FPS hot path on one GB300 (one JSON line on stdout).
+
+Workload (default "batched-256"): 256 seeded synthetic clouds, N log-uniform
+in [1,024, 131,072], D=3 uniform in a box with a per-cloud per-axis scale in
+[0.1, 10], K = N // 4, start_idx 0, QuickFPS (bucket_fps_kdline) with the
+tree height picked per size class.  One step = all 256 clouds sampled.
+
+  value   clouds/s with every cloud already resident in HBM (device entry
+          point), L2 flushed before each step, timed with CUDA events on the
+          launching stream; max over ranks.
+  e2e     clouds/s through the public drop-in API from host numpy arrays
+          (fpsample_gb300.bucket_fps_kdline_sampling), host<->device copies
+          inside the timed region.
+  roofline  the sampling kernel: algorithmic bytes per launch (bounding boxes
+          tested x (8D+8) B + running distances recomputed x (4D+8) B, both
+          counted on the device) / its event-timed average launch duration,
+          against the measured HBM copy bandwidth.
+  cpu_baseline  the oracle (C restatement of the reference, or the reference
+          compiled from its sources where present) on a bounded sample, 1 core.
+
+--impl reference runs the reference's CPU implementation of the same path on
+all host cores (rank 0 only) and prints the same metric.
+Multi-GPU (torchrun): replicas only -- every rank samples its own copy of the
+batch; value = all clouds / max step time over ranks ("weak" scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "clouds/sec"
+UNIT = "clouds/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def h_for(n: int) -> int:
+    """Tree height by size class (the reference README's guidance: h=5 for small
+    clouds, 7 for medium, 9 for large)."""
+    if n < 8192:
+        return 5
+    if n < 262144:
+        return 7
+    return 9
+
+
+def workload(name: str):
+    from fpsample_gb300 import workloads as W
+
+    if name == "batched-256":
+        clouds = W.batched_clouds(seed=W.SEEDS["batched-256"])
+        return [(p, k, h_for(p.shape[0]), 0) for p, k in clouds]
+    if name == "gmm-1m":
+        p = W.gmm_cloud(1 << 20, seed=W.SEEDS["gmm-1m"])
+        return [(p, 16384, 7, 0)]
+    if name == "single-4k":
+        p = W.uniform_cloud(4096, 3, seed=W.SEEDS["single-4k"])
+        return [(p, 1024, 5, 0)]
+    raise ValueError(name)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    def __init__(self, gpu_index: int):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={CLOCK_FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# CPU side: oracle / reference
+# ---------------------------------------------------------------------------
+def _cpu_impl():
+    """('reference', module) when the reference compiled from its own sources
+    is importable here, else ('port', Oracle)."""
+    from oracle import oracle as O
+
+    mode = os.environ.get("FPSAMPLE_FP_MODE", "nofma")
+    if O.reference_available(mode):
+        return "reference", O.load_reference(mode)
+    return "port", O.Oracle()
+
+
+def _cpu_run(impl, obj, pts, k, h, start):
+    mode = os.environ.get("FPSAMPLE_FP_MODE", "nofma")
+    if impl == "reference":
+        return obj.bucket_fps_kdline_sampling(pts, k, h, start)
+    return obj.kdline(pts, k, h, start, mode)
+
+
+_W = {}
+
+
+def _worker_init(name):
+    sys.path.insert(0, ROOT)
+    _W["clouds"] = workload(name)
+    _W["impl"], _W["obj"] = _cpu_impl()
+
+
+def _worker_run(i):
+    p, k, h, s = _W["clouds"][i]
+    _cpu_run(_W["impl"], _W["obj"], p, k, h, s)
+    return i
+
+
+def cpu_baseline(clouds, budget_s: float = 12.0):
+    impl, obj = _cpu_impl()
+    t0 = time.perf_counter()
+    done = 0
+    pts_done = 0
+    for p, k, h, s in clouds:
+        _cpu_run(impl, obj, p, k, h, s)
+        done += 1
+        pts_done += p.shape[0]
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": UNIT, "cores": 1, "kind": impl,
+            "sample": f"first {done} of {len(clouds)} clouds ({pts_done} points), one thread, "
+                      f"{dt:.1f} s"}
+
+
+def run_reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+
+    clouds = workload(args.workload)
+    impl, _ = _cpu_impl()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    # largest clouds first so that the pool drains evenly
+    order = sorted(range(len(clouds)), key=lambda i: -clouds[i][0].shape[0] * clouds[i][1])
+    with ctx.Pool(cores, initializer=_worker_init, initargs=(args.workload,)) as pool:
+        for _ in range(args.warmup):
+            list(pool.imap_unordered(_worker_run, order))
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            list(pool.imap_unordered(_worker_run, order))
+            times.append(time.perf_counter() - t0)
+    step = statistics.mean(times)
+    v = len(clouds) / step
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generators)",
+            "config": config_of(args.workload, clouds),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": impl,
+                             "sample": f"all {len(clouds)} clouds per step, {cores} processes"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_of(name, clouds):
+    ns = [p.shape[0] for p, _, _, _ in clouds]
+    return {"workload": name, "n_clouds": len(clouds), "points_total": int(sum(ns)),
+            "samples_total": int(sum(k for _, k, _, _ in clouds)), "dim": 3,
+            "k": "N//4" if name == "batched-256" else int(clouds[0][1]),
+            "h": "size class: 5 (<8K), 7 (<256K), 9" if name == "batched-256" else clouds[0][2],
+            "start_idx": 0, "l2": "flushed before every step (256 MiB write)",
+            "parallelism": "replicas"}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu_arm(args):
+    import torch
+    import torch.distributed as dist
+
+    import fpsample_gb300 as fps
+    from fpsample_gb300 import capi
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+
+    clouds = workload(args.workload)
+    # inputs resident in HBM: one buffer, per-cloud views
+    sizes = [p.shape[0] for p, _, _, _ in clouds]
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    host_all = np.concatenate([p for p, _, _, _ in clouds]).astype(np.float32)
+    d_all = torch.from_numpy(host_all).to(dev)
+    ks = [k for _, k, _, _ in clouds]
+    koffs = np.concatenate([[0], np.cumsum(ks)])
+    d_out = torch.empty(int(koffs[-1]), dtype=torch.int64, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    base_pts = d_all.data_ptr()
+    base_out = d_out.data_ptr()
+    sptr = stream.cuda_stream
+
+    def step_device():
+        for i, (p, k, h, s) in enumerate(clouds):
+            capi.kdline_device(base_pts + int(offs[i]) * 12, sizes[i], 3, k, s, h,
+                               base_out + int(koffs[i]) * 8, 0, sptr)
+
+    def step_e2e():
+        for p, k, h, s in clouds:
+            fps.bucket_fps_kdline_sampling(p, k, h, s)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    # correctness of what is timed: a few clouds against the oracle (outside timing)
+    from oracle.oracle import Oracle
+
+    orc = Oracle()
+    step_device()
+    torch.cuda.synchronize()
+    res = d_out.cpu().numpy().astype(np.uint64)
+    check_ids = sorted(set([0, 1, len(clouds) // 2, int(np.argmax(sizes))]))
+    bit_exact = True
+    for i in check_ids:
+        p, k, h, s = clouds[i]
+        want = orc.kdline(p, k, h, s, fps.get_fp_mode())
+        bit_exact &= bool(np.array_equal(res[koffs[i]:koffs[i + 1]], want))
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        step_device()
+    barrier()
+
+    capi.stats_reset()
+    capi.stats_timing(True)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        barrier()
+        t_wall = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            step_device()
+            ev[i][1].record(stream)
+        barrier()
+        t_wall = time.perf_counter() - t_wall
+    capi.stats_timing(False)
+    st = capi.stats()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    my_ms = statistics.mean(step_ms)
+    t = torch.tensor([my_ms], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    value = len(clouds) * world / (ms / 1e3)
+
+    # e2e through the public API (host arrays, copies inside the timed region)
+    e2e_steps = max(1, min(args.steps, 3))
+    step_e2e()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        step_e2e()
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    te = torch.tensor([e2e_s], device=dev)
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_v = len(clouds) * world / float(te.item())
+
+    if rank == 0:
+        launches = int(st["kernel_launches"])
+        d = 3
+        alg_bytes = st["pieces_tested"] * (8 * d + 8) + st["points_touched"] * (4 * d + 8)
+        per_launch_bytes = alg_bytes / max(1, st["sampler_launches"])
+        per_launch_ms = st["sampler_ms"] / max(1, st["sampler_launches"])
+        achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else None
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except OSError:
+            pass
+        peak = peaks.get("hbm_gbs", 6800.0)
+        traffic = None
+        tpath = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tpath):
+            tj = json.load(open(tpath)).get(args.workload)
+            if tj:
+                traffic = tj.get("dram_bytes_per_launch")
+        cpu = cpu_baseline(clouds) if world == 1 or rank == 0 else None
+        lat = sorted(step_ms)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generators, fpsample_gb300.workloads)",
+            "config": config_of(args.workload, clouds),
+            "bit_exact_checked_clouds": check_ids, "bit_exact": bit_exact,
+            "e2e": {"value": e2e_v, "unit": UNIT,
+                    "h2d_bytes_per_step": int(host_all.nbytes),
+                    "d2h_bytes_per_step": int(koffs[-1]) * 8},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "kernel": "sampler", "alg_bytes_per_launch": per_launch_bytes,
+                         "launch_ms": per_launch_ms,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+            "step_ms": {"min": lat[0], "median": statistics.median(lat), "max": lat[-1]},
+            "wall_s_timed_region": t_wall,
+            "stats": st,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="batched-256",
+                    choices=["batched-256", "gmm-1m", "single-4k"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

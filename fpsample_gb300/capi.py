@@ -29,11 +29,39 @@ SIGNATURES = {
     "fpsgpu_kdline_build": (ctypes.c_int, [_f32p, _sz, _sz, _sz, _u64p, _u64p, _szp]),
     "fpsgpu_set_fp_mode": (ctypes.c_int, [ctypes.c_int]),
     "fpsgpu_get_fp_mode": (ctypes.c_int, []),
+    "fpsgpu_stats_reset": (None, []),
+    "fpsgpu_stats_get": (None, [ctypes.c_void_p]),
+    "fpsgpu_stats_timing": (None, [ctypes.c_int]),
     "fpsgpu_last_error": (ctypes.c_char_p, []),
     "fpsgpu_version": (ctypes.c_char_p, []),
 }
 
 FP_MODES = {"nofma": 0, "fma": 1}
+
+
+class Stats(ctypes.Structure):
+    """fpsgpu_stats (include/fpsgpu.h)."""
+
+    _fields_ = [("kernel_launches", ctypes.c_uint64), ("sampler_launches", ctypes.c_uint64),
+                ("sampler_ms", ctypes.c_double), ("samples", ctypes.c_uint64),
+                ("pieces_tested", ctypes.c_uint64), ("points_touched", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+def stats_reset() -> None:
+    lib().fpsgpu_stats_reset()
+
+
+def stats_timing(enable: bool) -> None:
+    lib().fpsgpu_stats_timing(1 if enable else 0)
+
+
+def stats() -> dict:
+    s = Stats()
+    lib().fpsgpu_stats_get(ctypes.byref(s))
+    return s.as_dict()
 
 
 class FpsGpuError(RuntimeError):

@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -66,6 +67,7 @@ int current_ctx(DevCtx* out) {
 
 int launch_persistent(const void* func, int grid, int block, void** args, size_t smem,
                       cudaStream_t stream, bool cooperative) {
+    stats_count_launch();
     if (cooperative) {
         int dev = 0, sms = 0, per_sm = 0;
         FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
@@ -80,6 +82,57 @@ int launch_persistent(const void* func, int grid, int block, void** args, size_t
         FPSGPU_CUDA_TRY(cudaLaunchKernel(func, dim3(grid), dim3(block), args, smem, stream));
     }
     return FPSGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// measurement counters
+// ---------------------------------------------------------------------------
+namespace {
+std::mutex g_stats_mu;
+fpsgpu_stats g_stats{};
+std::atomic<int> g_timing{0};
+}  // namespace
+
+void stats_count_launch(uint64_t n) {
+    std::lock_guard<std::mutex> lk(g_stats_mu);
+    g_stats.kernel_launches += n;
+}
+
+bool stats_timing_enabled() { return g_timing.load() != 0; }
+
+void SamplerTimer::begin(cudaStream_t s) {
+    on = stats_timing_enabled();
+    if (!on) return;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        on = false;
+        return;
+    }
+    cudaEventRecord(e0, s);
+}
+
+void SamplerTimer::end(cudaStream_t s) {
+    if (on) cudaEventRecord(e1, s);
+}
+
+void SamplerTimer::finish(uint64_t samples, const uint64_t* c) {
+    float ms = 0.0f;
+    if (on) {
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+    }
+    std::lock_guard<std::mutex> lk(g_stats_mu);
+    g_stats.sampler_launches += 1;
+    g_stats.sampler_ms += ms;
+    g_stats.samples += samples;
+    if (c) {
+        g_stats.pieces_tested += c[0];
+        g_stats.points_touched += c[1];
+    }
+}
+
+SamplerTimer::~SamplerTimer() {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
 }
 
 // ---------------------------------------------------------------------------
@@ -171,6 +224,7 @@ int kd_compact(const uint8_t* flag, uint64_t n, uint32_t piece, uint32_t* starts
     uint32_t* bcount;
     int rc;
     if ((rc = sc.alloc(&bcount, nblocks))) return rc;
+    stats_count_launch(3);
     compact_count<<<(unsigned)nblocks, 1024, 0, stream>>>(flag, n, piece, bcount);
     FPSGPU_CUDA_TRY(cudaGetLastError());
     compact_scan<<<1, 1024, 0, stream>>>(bcount, (uint32_t)nblocks, d_count);
@@ -268,6 +322,18 @@ int kdline_device_impl(const float* d_points, size_t n, size_t dim, size_t k, si
 }  // namespace
 
 extern "C" {
+
+void fpsgpu_stats_reset(void) {
+    std::lock_guard<std::mutex> lk(g_stats_mu);
+    g_stats = fpsgpu_stats{};
+}
+
+void fpsgpu_stats_get(fpsgpu_stats* out) {
+    std::lock_guard<std::mutex> lk(g_stats_mu);
+    *out = g_stats;
+}
+
+void fpsgpu_stats_timing(int enable) { g_timing.store(enable ? 1 : 0); }
 
 const char* fpsgpu_last_error(void) { return t_last_error.c_str(); }
 

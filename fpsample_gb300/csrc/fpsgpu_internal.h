@@ -95,6 +95,21 @@ struct KdlineCall {
 int run_kdline_nofma(const KdlineCall& c);
 int run_kdline_fma(const KdlineCall& c);
 
+// measurement counters (fpsgpu_stats_*)
+void stats_count_launch(uint64_t n = 1);
+bool stats_timing_enabled();
+// Records the sampler's events/counters: call begin() right before the sampler
+// launch and end() right after it (same stream); end() adds the device time
+// after the caller's stream synchronisation via finish().
+struct SamplerTimer {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    bool on = false;
+    void begin(cudaStream_t s);
+    void end(cudaStream_t s);
+    void finish(uint64_t samples, const uint64_t* h_counters /* tested, touched */);
+    ~SamplerTimer();
+};
+
 // cooperative launch helper: refuses grids that cannot be co-resident
 int launch_persistent(const void* func, int grid, int block, void** args, size_t smem,
                       cudaStream_t stream, bool cooperative);

@@ -406,6 +406,7 @@ struct KdSampleArgs {
     float* trace;
     uint64_t* slots;
     int* err;
+    unsigned long long* counters;  // [2]: boxes tested, distances recomputed
 };
 
 // Applies reference point r to the warp's pieces [q0, q1): INIT sets every
@@ -414,7 +415,7 @@ struct KdSampleArgs {
 // key over all its pieces (lowest position wins ties).
 template <int D, bool FMA, bool INIT>
 __device__ __forceinline__ uint64_t kd_apply(const KdSampleArgs& a, uint32_t q0, uint32_t q1,
-                                             const float* r) {
+                                             const float* r, unsigned long long& touched) {
     const int lane = threadIdx.x & 31;
     const uint64_t n = a.n;
     uint64_t wbest = 0;
@@ -439,6 +440,7 @@ __device__ __forceinline__ uint64_t kd_apply(const KdSampleArgs& a, uint32_t q0,
             m &= m - 1;
             const uint32_t qq = qb + l;
             const uint32_t ps = __ldg(a.pstart + qq), pe = __ldg(a.pstart + qq + 1);
+            touched += pe - ps;
             uint64_t pk = 0;
 #pragma unroll 2
             for (uint32_t p = ps + lane; p < pe; p += 32) {
@@ -490,12 +492,14 @@ __global__ void __launch_bounds__(kSampleThreads, 1) kd_sample(KdSampleArgs a) {
     __syncthreads();
 
     uint32_t xround = 0;
+    unsigned long long tested = 0, touched = 0;
     for (uint64_t t = 0; t + 1 < a.k; ++t) {
         float r[D];
 #pragma unroll
         for (int d = 0; d < D; ++d) r[d] = s_ref[d];
-        const uint64_t wbest = t == 0 ? kd_apply<D, FMA, true>(a, q0, q1, r)
-                                      : kd_apply<D, FMA, false>(a, q0, q1, r);
+        if (t > 0) tested += q1 - q0;
+        const uint64_t wbest = t == 0 ? kd_apply<D, FMA, true>(a, q0, q1, r, touched)
+                                      : kd_apply<D, FMA, false>(a, q0, q1, r, touched);
         if (lane == 0) s_wkey[warp] = wbest;
         __syncthreads();
         if (warp == 0) {
@@ -521,6 +525,10 @@ __global__ void __launch_bounds__(kSampleThreads, 1) kd_sample(KdSampleArgs a) {
         }
         __syncthreads();
         if (s_abort) break;
+    }
+    if (a.counters && lane == 0) {
+        atomicAdd(a.counters, tested);
+        atomicAdd(a.counters + 1, touched);
     }
 }
 
@@ -556,6 +564,7 @@ int run_kdline_d(const KdlineCall& c) {
     {
         uint64_t blocks = (n + 255) / 256;
         if (blocks > 8192) blocks = 8192;
+        stats_count_launch();
         kd_prepare<D><<<(unsigned)blocks, 256, 0, c.stream>>>(c.d_points, b, levels == 0 ? 1 : 0);
         FPSGPU_CUDA_TRY(cudaGetLastError());
     }
@@ -563,6 +572,7 @@ int run_kdline_d(const KdlineCall& c) {
     for (uint64_t j = 0; j < levels; ++j) {
         uint64_t grid = known_cnt;
         if (grid == 0) break;
+        stats_count_launch();
         kd_split_level<D><<<(unsigned)grid, kBuildThreads, 0, c.stream>>>(b, (uint32_t)j);
         FPSGPU_CUDA_TRY(cudaGetLastError());
         std::swap(b.nodes_cur, b.nodes_next);
@@ -626,6 +636,7 @@ int run_kdline_d(const KdlineCall& c) {
     {
         uint64_t blocks = (np_bound * 32 + 255) / 256;
         if (blocks > 4096) blocks = 4096;
+        stats_count_launch();
         piece_bbox<D><<<(unsigned)blocks, 256, 0, c.stream>>>(b.X, n, pstart, d_np, plo, phi);
         FPSGPU_CUDA_TRY(cudaGetLastError());
     }
@@ -653,13 +664,26 @@ int run_kdline_d(const KdlineCall& c) {
     s.trace = c.d_trace;
     s.slots = slots;
     s.err = b.err;
+    unsigned long long* counters;
+    if ((rc = sc.alloc(&counters, 2))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), c.stream));
+    s.counters = counters;
     void* args[] = {&s};
+    SamplerTimer timer;
+    timer.begin(c.stream);
     if ((rc = launch_persistent((const void*)kd_sample<D, FMA>, (int)G, kSampleThreads, args, 0,
                                 c.stream, G > 1)))
         return rc;
+    timer.end(c.stream);
     int h_err = 0;
+    unsigned long long h_cnt[2] = {0, 0};
     FPSGPU_CUDA_TRY(cudaMemcpyAsync(&h_err, b.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(h_cnt, counters, sizeof(h_cnt), cudaMemcpyDeviceToHost, c.stream));
     FPSGPU_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    {
+        const uint64_t cnt[2] = {h_cnt[0], h_cnt[1]};
+        timer.finish(c.k, cnt);
+    }
     if (h_err & kErrNonFiniteSplit)
         return set_error(FPSGPU_ERR_NONFINITE,
                          "kd-line build met a NaN coordinate in a split dimension");

@@ -286,6 +286,7 @@ int run_vanilla_d(const VanillaCall& c) {
         G = (int)g;
         (void)per_cta;
     }
+    SamplerTimer timer;
     if (resident) {
         uint64_t* slots = nullptr;
         if (G > 1) {
@@ -294,6 +295,7 @@ int run_vanilla_d(const VanillaCall& c) {
         }
         a.slots = slots;
         a.smem_cloud = (G == 1 && c.n * D * sizeof(float) <= 96 * 1024) ? 1 : 0;
+        timer.begin(c.stream);
         switch (ppt) {
             case 1: rc = launch_resident<DR, FMA, 1>(c, a, G); break;
             case 2: rc = launch_resident<DR, FMA, 2>(c, a, G); break;
@@ -301,6 +303,7 @@ int run_vanilla_d(const VanillaCall& c) {
             default: rc = launch_resident<DR, FMA, ppt_max>(c, a, G); break;
         }
         if (rc) return rc;
+        timer.end(c.stream);
     } else {
         G = max_g;
         float *X, *dis;
@@ -312,6 +315,7 @@ int run_vanilla_d(const VanillaCall& c) {
         {
             uint64_t blocks = (c.n + 255) / 256;
             if (blocks > 65535ull * 64) blocks = 65535ull * 64;
+            stats_count_launch();
             transpose_to_soa<<<(unsigned)blocks, 256, 0, c.stream>>>(c.d_points, X, c.n, c.dim);
             FPSGPU_CUDA_TRY(cudaGetLastError());
         }
@@ -324,13 +328,20 @@ int run_vanilla_d(const VanillaCall& c) {
             FPSGPU_CUDA_TRY(cudaFuncSetAttribute(
                 kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         void* args[] = {&a};
+        timer.begin(c.stream);
         if ((rc = launch_persistent((const void*)kern, G, kVanillaThreads, args, smem, c.stream,
                                     true)))
             return rc;
+        timer.end(c.stream);
     }
     int h_err = 0;
     FPSGPU_CUDA_TRY(cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     FPSGPU_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    {
+        // brute force: every running distance is recomputed on every iteration
+        const uint64_t cnt[2] = {0, c.k > 0 ? c.n * (c.k - 1) : 0};
+        timer.finish(c.k, cnt);
+    }
     if (h_err)
         return set_error(FPSGPU_ERR_DEVICE, "vanilla FPS kernel gave up (device error word 0x%x)",
                          h_err);

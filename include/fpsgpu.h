@@ -99,6 +99,30 @@ int fpsgpu_kdline_build(const float *raw_data, size_t n_points, size_t dim,
 int fpsgpu_set_fp_mode(int mode);
 int fpsgpu_get_fp_mode(void);
 
+/*
+ * Process-wide counters for measurement (all calls, all threads).
+ *   kernel_launches : kernels this library launched
+ *   sampler_launches: launches of the sampling kernels (the hot loop)
+ *   sampler_ms      : their summed device time, from CUDA events recorded on
+ *                     the launching stream; only while timing is enabled
+ *   samples         : points chosen by the sampling kernels
+ *   pieces_tested   : bounding-box tests made by the pruned sampler
+ *   points_touched  : running distances recomputed by the sampling kernels
+ */
+typedef struct {
+    uint64_t kernel_launches;
+    uint64_t sampler_launches;
+    double sampler_ms;
+    uint64_t samples;
+    uint64_t pieces_tested;
+    uint64_t points_touched;
+} fpsgpu_stats;
+
+void fpsgpu_stats_reset(void);
+void fpsgpu_stats_get(fpsgpu_stats *out);
+/* 1: record CUDA events around every sampler launch (adds a stream sync per call) */
+void fpsgpu_stats_timing(int enable);
+
 /* message describing the last failure on the calling thread ("" if none) */
 const char *fpsgpu_last_error(void);
 
