@@ -282,7 +282,8 @@ def run_gpu_arm(args):
     step_device()
     torch.cuda.synchronize()
     res = d_out.cpu().numpy().astype(np.uint64)
-    check_ids = sorted(set([0, 1, len(clouds) // 2, int(np.argmax(sizes))]))
+    check_ids = sorted(set(i for i in (0, 1, len(clouds) // 2, int(np.argmax(sizes)))
+                           if i < len(clouds)))
     bit_exact = True
     for i in check_ids:
         p, k, h, s = clouds[i]

@@ -11,11 +11,15 @@
 
 #include "fpsgpu_device.cuh"
 #include "fpsgpu_internal.h"
-#include "kdline.cuh"
+#include "engine.cuh"
 
 static_assert(sizeof(size_t) == sizeof(uint64_t), "size_t must be 64-bit");
 
 #define FPSGPU_VERSION_STRING "1.0.2+gb300.0.1"
+
+// vanilla FPS on at most this many points runs the single-CTA brute-force
+// kernel; larger clouds (dim <= 8) go through the pruned engine
+constexpr uint64_t kVanillaBruteMax = 8192;
 
 namespace fpsgpu {
 
@@ -145,12 +149,12 @@ __global__ void transpose_to_soa(const float* __restrict__ pts, float* __restric
         for (int d = 0; d < dim; ++d) X[(uint64_t)d * n + p] = pts[p * dim + d];
 }
 
-__global__ void compact_count(const uint8_t* flag, uint64_t n, uint32_t piece, uint32_t* bcount) {
+__global__ void compact_count(const uint8_t* flag, uint64_t n, uint32_t* bcount) {
     const uint64_t lo = (uint64_t)blockIdx.x * kCompactChunk;
     uint64_t hi = lo + kCompactChunk;
     if (hi > n) hi = n;
     uint32_t c = 0;
-    for (uint64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) c += run_start(flag, p, piece);
+    for (uint64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) c += run_start(flag, p);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
     __shared__ uint32_t s[32];
@@ -171,9 +175,8 @@ __global__ void compact_scan(uint32_t* bcount, uint32_t nblocks, uint32_t* total
     for (uint32_t base = 0; base < nblocks; base += blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         const uint32_t v = i < nblocks ? bcount[i] : 0u;
-        // block exclusive scan of v (values may exceed 1: scan warp sums)
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-        uint32_t x = v;
+        uint32_t x = v;  // inclusive scan within the warp
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             uint32_t u = __shfl_up_sync(kFull, x, o);
@@ -198,8 +201,8 @@ __global__ void compact_scan(uint32_t* bcount, uint32_t nblocks, uint32_t* total
     if (threadIdx.x == 0) *total = carry;
 }
 
-__global__ void compact_write(const uint8_t* flag, uint64_t n, uint32_t piece,
-                              const uint32_t* boff, const uint32_t* total, uint32_t* starts) {
+__global__ void compact_write(const uint8_t* flag, uint64_t n, const uint32_t* boff,
+                              const uint32_t* total, uint32_t* starts) {
     __shared__ uint32_t s_w[64];
     const uint64_t lo = (uint64_t)blockIdx.x * kCompactChunk;
     uint64_t hi = lo + kCompactChunk;
@@ -208,7 +211,7 @@ __global__ void compact_write(const uint8_t* flag, uint64_t n, uint32_t piece,
     int par = 0;
     for (uint64_t base = lo; base < hi; base += blockDim.x) {
         const uint64_t p = base + threadIdx.x;
-        const bool f = p < hi && run_start(flag, p, piece);
+        const bool f = p < hi && run_start(flag, p);
         uint32_t tot;
         const uint32_t r = block_rank(f, s_w, par, tot);
         par ^= 1;
@@ -218,20 +221,27 @@ __global__ void compact_write(const uint8_t* flag, uint64_t n, uint32_t piece,
     if (blockIdx.x == 0 && threadIdx.x == 0) starts[*total] = (uint32_t)n;
 }
 
-int kd_compact(const uint8_t* flag, uint64_t n, uint32_t piece, uint32_t* starts,
-               uint32_t* d_count, Scratch& sc, cudaStream_t stream) {
+int compact_flags(const uint8_t* flag, uint64_t n, uint32_t* starts, uint32_t* d_count,
+                  Scratch& sc, cudaStream_t stream) {
     const uint64_t nblocks = (n + kCompactChunk - 1) / kCompactChunk;
     uint32_t* bcount;
     int rc;
     if ((rc = sc.alloc(&bcount, nblocks))) return rc;
     stats_count_launch(3);
-    compact_count<<<(unsigned)nblocks, 1024, 0, stream>>>(flag, n, piece, bcount);
+    compact_count<<<(unsigned)nblocks, 1024, 0, stream>>>(flag, n, bcount);
     FPSGPU_CUDA_TRY(cudaGetLastError());
     compact_scan<<<1, 1024, 0, stream>>>(bcount, (uint32_t)nblocks, d_count);
     FPSGPU_CUDA_TRY(cudaGetLastError());
-    compact_write<<<(unsigned)nblocks, 1024, 0, stream>>>(flag, n, piece, bcount, d_count, starts);
+    compact_write<<<(unsigned)nblocks, 1024, 0, stream>>>(flag, n, bcount, d_count, starts);
     FPSGPU_CUDA_TRY(cudaGetLastError());
     return FPSGPU_OK;
+}
+
+__global__ void build_seed_refine(BuildArgs a) {
+    const uint32_t m = *a.refine_cnt;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+        a.cur[i] = a.refine[i];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.cnt_cur = m;
 }
 
 // ---------------------------------------------------------------------------
@@ -278,6 +288,20 @@ int fps_device_impl(const float* d_points, size_t n, size_t dim, size_t k, const
     c.d_trace = d_trace;
     c.stream = stream;
     c.sms = sms;
+    if (dim <= 8 && n > kVanillaBruteMax) {
+        EngineCall e{};
+        e.d_points = d_points;
+        e.n = n;
+        e.k = k;
+        e.kd = false;
+        e.h_forced = reinterpret_cast<const uint64_t*>(h_start);
+        e.n_forced = (uint32_t)n_start;
+        e.d_out = d_out;
+        e.d_trace = d_trace;
+        e.stream = stream;
+        e.sms = sms;
+        return fp_mode() == FPSGPU_FP_FMA ? run_engine_fma((int)dim, e) : run_engine_nofma((int)dim, e);
+    }
     return fp_mode() == FPSGPU_FP_FMA ? run_vanilla_fma(c) : run_vanilla_nofma(c);
 }
 
@@ -305,18 +329,20 @@ int check_kdline_args(size_t n, size_t dim, size_t start) {
 
 int kdline_device_impl(const float* d_points, size_t n, size_t dim, size_t k, size_t start,
                        size_t height, uint64_t* d_out, float* d_trace, cudaStream_t stream, int sms) {
-    KdlineCall c{};
+    const uint64_t forced = start;
+    EngineCall c{};
     c.d_points = d_points;
     c.n = n;
-    c.dim = (int)dim;
     c.k = k;
-    c.start = start;
+    c.kd = true;
     c.height = height;
+    c.h_forced = &forced;
+    c.n_forced = 1;
     c.d_out = d_out;
     c.d_trace = d_trace;
     c.stream = stream;
     c.sms = sms;
-    return fp_mode() == FPSGPU_FP_FMA ? run_kdline_fma(c) : run_kdline_nofma(c);
+    return fp_mode() == FPSGPU_FP_FMA ? run_engine_fma((int)dim, c) : run_engine_nofma((int)dim, c);
 }
 
 }  // namespace
@@ -439,17 +465,20 @@ int fpsgpu_kdline_build(const float* raw_data, size_t n_points, size_t dim, size
     if ((rc = sc.alloc(&d_pts, n_points * dim))) return rc;
     FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_pts, raw_data, n_points * dim * sizeof(float),
                                     cudaMemcpyHostToDevice, ctx.stream));
-    KdlineCall c{};
+    const uint64_t forced = 0;
+    EngineCall c{};
     c.d_points = d_pts;
     c.n = n_points;
-    c.dim = (int)dim;
+    c.kd = true;
     c.height = height;
+    c.h_forced = &forced;
+    c.n_forced = 1;
     c.stream = ctx.stream;
     c.sms = ctx.sms;
     c.h_perm = h_perm;
     c.h_bucket_start = h_bucket_start;
     c.h_n_buckets = n_buckets;
-    return fp_mode() == FPSGPU_FP_FMA ? run_kdline_fma(c) : run_kdline_nofma(c);
+    return fp_mode() == FPSGPU_FP_FMA ? run_engine_fma((int)dim, c) : run_engine_nofma((int)dim, c);
 }
 
 }  // extern "C"

@@ -1,0 +1,6 @@
+// Pruned FPS engine (kd-line and vanilla) instantiated for the fma floating-point mode.
+#include "engine.cuh"
+
+namespace fpsgpu {
+int run_engine_fma(int dim, const EngineCall& c) { return run_engine_dispatch<true>(dim, c); }
+}  // namespace fpsgpu

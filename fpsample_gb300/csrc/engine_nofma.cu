@@ -1,0 +1,6 @@
+// Pruned FPS engine (kd-line and vanilla) instantiated for the nofma floating-point mode.
+#include "engine.cuh"
+
+namespace fpsgpu {
+int run_engine_nofma(int dim, const EngineCall& c) { return run_engine_dispatch<false>(dim, c); }
+}  // namespace fpsgpu

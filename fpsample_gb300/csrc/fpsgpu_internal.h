@@ -75,25 +75,10 @@ struct VanillaCall {
 int run_vanilla_nofma(const VanillaCall& c);
 int run_vanilla_fma(const VanillaCall& c);
 
-// One kd-line QuickFPS call on device buffers.
-struct KdlineCall {
-    const float* d_points;  // row-major [n][dim]
-    uint64_t n;
-    int dim;
-    uint64_t k;
-    uint64_t start;
-    uint64_t height;
-    uint64_t* d_out;
-    float* d_trace;
-    cudaStream_t stream;
-    int sms;
-    // build-only mode (k ignored): host outputs
-    uint64_t* h_perm;
-    uint64_t* h_bucket_start;
-    size_t* h_n_buckets;
-};
-int run_kdline_nofma(const KdlineCall& c);
-int run_kdline_fma(const KdlineCall& c);
+// The pruned engine (engine.cuh): kd-line QuickFPS and vanilla FPS.
+struct EngineCall;
+int run_engine_nofma(int dim, const EngineCall& c);
+int run_engine_fma(int dim, const EngineCall& c);
 
 // measurement counters (fpsgpu_stats_*)
 void stats_count_launch(uint64_t n = 1);
