@@ -261,14 +261,23 @@ def run_gpu_arm(args):
     base_out = d_out.data_ptr()
     sptr = stream.cuda_stream
 
+    hs = [h for _, _, h, _ in clouds]
+    ss = [s for _, _, _, s in clouds]
+
     def step_device():
+        # the batched engine: every cloud in one call
+        capi.kdline_batch_device(base_pts, offs, 3, ks, hs, ss, base_out, sptr)
+
+    def step_plain():
+        # the plain form: one GPU call per cloud
         for i, (p, k, h, s) in enumerate(clouds):
             capi.kdline_device(base_pts + int(offs[i]) * 12, sizes[i], 3, k, s, h,
                                base_out + int(koffs[i]) * 8, 0, sptr)
 
+    pcs = [p for p, _, _, _ in clouds]
+
     def step_e2e():
-        for p, k, h, s in clouds:
-            fps.bucket_fps_kdline_sampling(p, k, h, s)
+        fps.bucket_fps_kdline_sampling_batch(pcs, ks, hs, ss)
 
     def barrier():
         torch.cuda.synchronize()
@@ -333,6 +342,18 @@ def run_gpu_arm(args):
         dist.all_reduce(te, op=dist.ReduceOp.MAX)
     e2e_v = len(clouds) * world / float(te.item())
 
+    # the plain one-call-per-cloud GPU form on the same data, for comparison
+    barrier()
+    pe0 = torch.cuda.Event(enable_timing=True)
+    pe1 = torch.cuda.Event(enable_timing=True)
+    flush.zero_()
+    pe0.record(stream)
+    step_plain()
+    pe1.record(stream)
+    barrier()
+    plain_ms = pe0.elapsed_time(pe1)
+    plain_ok = bool(np.array_equal(d_out.cpu().numpy().astype(np.uint64), res))
+
     if rank == 0:
         launches = int(st["kernel_launches"])
         d = 3
@@ -361,6 +382,9 @@ def run_gpu_arm(args):
             "data": "synthetic (seeded generators, fpsample_gb300.workloads)",
             "config": config_of(args.workload, clouds),
             "bit_exact_checked_clouds": check_ids, "bit_exact": bit_exact,
+            "plain_per_cloud": {"value": len(clouds) / (plain_ms / 1e3), "unit": UNIT,
+                                "ms_per_step": plain_ms, "identical_to_batched": plain_ok,
+                                "batched_speedup": plain_ms / ms},
             "e2e": {"value": e2e_v, "unit": UNIT,
                     "h2d_bytes_per_step": int(host_all.nbytes),
                     "d2h_bytes_per_step": int(koffs[-1]) * 8},

@@ -31,6 +31,7 @@ try:
         __doc__ as _ext_doc,
         __version__,
         _bucket_fps_kdline_sampling,
+        _bucket_fps_kdline_sampling_batch,
         _bucket_fps_kdtree_sampling,
         _fps_npdu_kdtree_sampling,
         _fps_npdu_sampling,
@@ -118,6 +119,45 @@ def bucket_fps_kdline_sampling(
     return _bucket_fps_kdline_sampling(pc, n_samples, h, start_idx)
 
 
+def bucket_fps_kdline_sampling_batch(pcs, n_samples, h, start_idx=0):
+    """
+    Many clouds in one GPU call (no counterpart in the reference): the result
+    for every cloud is identical to ``bucket_fps_kdline_sampling`` on it alone.
+
+    Args:
+        pcs (list[np.ndarray]): point clouds of shape (n_i, D), same D <= 8.
+        n_samples (int or list[int]): samples per cloud.
+        h (int or list[int]): tree height per cloud.
+        start_idx (int or list[int], default=0): start per cloud (no random start).
+
+    Returns:
+        list[np.ndarray]: uint64 indices per cloud.
+    """
+    m = len(pcs)
+    ks = [n_samples] * m if isinstance(n_samples, int) else list(n_samples)
+    hs = [h] * m if isinstance(h, int) else list(h)
+    ss = [start_idx] * m if isinstance(start_idx, int) else list(start_idx)
+    assert len(ks) == m and len(hs) == m and len(ss) == m, "one value per cloud"
+    if m == 0:
+        return []
+    dims = {np.asarray(p).shape[1] for p in pcs}
+    assert len(dims) == 1, "all clouds must have the same dimension"
+    for p, k, hh, s in zip(pcs, ks, hs, ss):
+        n_pts = np.asarray(p).shape[0]
+        assert np.asarray(p).ndim == 2
+        assert 1 <= k <= n_pts, "n_pts should be >= n_samples >= 1"
+        assert hh >= 1, "h should be >= 1"
+        assert 2**hh <= n_pts, "2**h should be <= n_pts"
+        assert 0 <= s < n_pts, "0 <= start_idx < n_pts"
+    sizes = np.array([np.asarray(p).shape[0] for p in pcs], dtype=np.uint64)
+    offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    pts = np.ascontiguousarray(np.concatenate([np.asarray(p, dtype=np.float32) for p in pcs]))
+    out = _bucket_fps_kdline_sampling_batch(pts, offsets, np.array(ks, np.uint64),
+                                            np.array(hs, np.uint64), np.array(ss, np.uint64))
+    bounds = np.concatenate([[0], np.cumsum(ks)])
+    return [out[bounds[i]:bounds[i + 1]] for i in range(m)]
+
+
 def fps_npdu_sampling(pc, n_samples, w=None, start_idx=None):
     """Not part of the GB300 build (heuristic NPDU variant); raises NotImplementedError."""
     return _fps_npdu_sampling(pc, n_samples, w, start_idx)
@@ -161,6 +201,7 @@ __all__ = [
     "fps_npdu_kdtree_sampling",
     "bucket_fps_kdtree_sampling",
     "bucket_fps_kdline_sampling",
+    "bucket_fps_kdline_sampling_batch",
     "set_fp_mode",
     "get_fp_mode",
     "kdline_build",

@@ -27,6 +27,8 @@ SIGNATURES = {
     "fpsgpu_kdline_device": (ctypes.c_int, [_vp, _sz, _sz, _sz, _sz, _sz, _vp, _vp, _vp]),
     "fpsgpu_fps_device": (ctypes.c_int, [_vp, _sz, _sz, _sz, _szp, _sz, _vp, _vp, _vp]),
     "fpsgpu_kdline_build": (ctypes.c_int, [_f32p, _sz, _sz, _sz, _u64p, _u64p, _szp]),
+    "fpsgpu_kdline_batch": (ctypes.c_int, [_f32p, _szp, _sz, _sz, _szp, _szp, _szp, _szp]),
+    "fpsgpu_kdline_batch_device": (ctypes.c_int, [_vp, _szp, _sz, _sz, _szp, _szp, _szp, _vp, _vp]),
     "fpsgpu_set_fp_mode": (ctypes.c_int, [ctypes.c_int]),
     "fpsgpu_get_fp_mode": (ctypes.c_int, []),
     "fpsgpu_stats_reset": (None, []),
@@ -187,3 +189,33 @@ def fps_tensor(points, n_samples: int, starts=0, trace: bool = False):
         fps_device(pts.data_ptr(), pts.shape[0], pts.shape[1], n_samples, starts, out.data_ptr(),
                    tr.data_ptr() if trace else 0, stream)
     return (out, tr) if trace else out
+
+
+def kdline_batch(pcs, n_samples, heights, starts):
+    """Host-buffer batched QuickFPS through the C ABI; list of uint64 arrays."""
+    sizes = [np.asarray(p).shape[0] for p in pcs]
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    pts = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float32) for p in pcs]))
+    ks = np.asarray(n_samples, np.uint64)
+    out = np.zeros(int(ks.sum()), np.uint64)
+    hs = np.asarray(heights, np.uint64)
+    ss = np.asarray(starts, np.uint64)
+    rc = lib().fpsgpu_kdline_batch(pts.ctypes.data_as(_f32p), off.ctypes.data_as(_szp), len(pcs),
+                                   pts.shape[1], ks.ctypes.data_as(_szp), ss.ctypes.data_as(_szp),
+                                   hs.ctypes.data_as(_szp), out.ctypes.data_as(_szp))
+    _check("fpsgpu_kdline_batch", rc)
+    b = np.concatenate([[0], np.cumsum(ks)]).astype(np.int64)
+    return [out[b[i]:b[i + 1]] for i in range(len(pcs))]
+
+
+def kdline_batch_device(points_ptr: int, offsets, dim: int, n_samples, heights, starts,
+                        out_ptr: int, stream: int = 0) -> None:
+    """Device buffers (points [sum n, dim] float32, out [sum k] uint64); host per-cloud arrays."""
+    off = np.ascontiguousarray(offsets, np.uint64)
+    ks = np.ascontiguousarray(n_samples, np.uint64)
+    hs = np.ascontiguousarray(heights, np.uint64)
+    ss = np.ascontiguousarray(starts, np.uint64)
+    rc = lib().fpsgpu_kdline_batch_device(points_ptr, off.ctypes.data_as(_szp), len(ks), dim,
+                                          ks.ctypes.data_as(_szp), ss.ctypes.data_as(_szp),
+                                          hs.ctypes.data_as(_szp), out_ptr, stream or None)
+    _check("fpsgpu_kdline_batch_device", rc)

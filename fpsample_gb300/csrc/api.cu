@@ -72,6 +72,8 @@ int current_ctx(DevCtx* out) {
 int launch_persistent(const void* func, int grid, int block, void** args, size_t smem,
                       cudaStream_t stream, bool cooperative) {
     stats_count_launch();
+    if (cooperative && grid > kMaxGrid)
+        return set_error(FPSGPU_ERR_ARG, "persistent grid of %d CTAs exceeds %d", grid, kMaxGrid);
     if (cooperative) {
         int dev = 0, sms = 0, per_sm = 0;
         FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
@@ -235,6 +237,22 @@ int compact_flags(const uint8_t* flag, uint64_t n, uint32_t* starts, uint32_t* d
     compact_write<<<(unsigned)nblocks, 1024, 0, stream>>>(flag, n, bcount, d_count, starts);
     FPSGPU_CUDA_TRY(cudaGetLastError());
     return FPSGPU_OK;
+}
+
+__global__ void cloud_piece_ranges(const uint32_t* pstart, const uint32_t* npieces,
+                                   const uint64_t* cloud_off, uint32_t n_clouds, uint32_t* out) {
+    const uint32_t np = *npieces;
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c <= n_clouds;
+         c += gridDim.x * blockDim.x) {
+        const uint64_t key = cloud_off[c];
+        uint32_t lo = 0, hi = np;  // first piece whose start >= key
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) / 2;
+            if ((uint64_t)pstart[mid] < key) lo = mid + 1;
+            else hi = mid;
+        }
+        out[c] = lo;
+    }
 }
 
 __global__ void build_seed_refine(BuildArgs a) {
@@ -447,6 +465,70 @@ int bucket_fps_kdline(const float* raw_data, size_t n_points, size_t dim, size_t
                                  ctx.stream, ctx.sms)))
         return rc;
     FPSGPU_CUDA_TRY(cudaMemcpyAsync(sampled_point_indices, d_out, n_samples * sizeof(uint64_t),
+                                    cudaMemcpyDeviceToHost, ctx.stream));
+    FPSGPU_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
+    return FPSGPU_OK;
+}
+
+int fpsgpu_kdline_batch_device(const float* d_points, const size_t* h_offsets, size_t n_clouds,
+                               size_t dim, const size_t* h_n_samples, const size_t* h_start_idx,
+                               const size_t* h_height, uint64_t* d_out, void* stream) {
+    clear_error();
+    if (n_clouds == 0) return FPSGPU_OK;
+    if (!h_offsets || !h_n_samples || !h_start_idx || !h_height)
+        return set_error(FPSGPU_ERR_ARG, "null argument");
+    if (dim == 0 || dim > 8) return set_error(FPSGPU_ERR_DIM, "dim must be in [1, 8], got %zu", dim);
+    if (h_offsets[0] != 0) return set_error(FPSGPU_ERR_ARG, "offsets[0] must be 0");
+    if (h_offsets[n_clouds] > 0xfffffffeull)
+        return set_error(FPSGPU_ERR_ARG, "at most 2^32 - 2 points in one batch");
+    for (size_t c = 0; c < n_clouds; ++c) {
+        const size_t nc = h_offsets[c + 1] - h_offsets[c];
+        if (h_offsets[c + 1] < h_offsets[c] || nc == 0)
+            return set_error(FPSGPU_ERR_ARG, "cloud %zu is empty or offsets decrease", c);
+        if (h_start_idx[c] >= nc)
+            return set_error(FPSGPU_ERR_START, "cloud %zu: start_idx %zu out of range (n=%zu)", c,
+                             h_start_idx[c], nc);
+    }
+    DevCtx ctx;
+    cudaStream_t s;
+    int rc;
+    if ((rc = resolve_stream(stream, &ctx, &s))) return rc;
+    BatchCall b;
+    b.d_points = d_points;
+    b.off.assign(h_offsets, h_offsets + n_clouds + 1);
+    b.k.assign(h_n_samples, h_n_samples + n_clouds);
+    b.start.assign(h_start_idx, h_start_idx + n_clouds);
+    b.height.assign(h_height, h_height + n_clouds);
+    b.kd = true;
+    b.d_out = d_out;
+    b.stream = s;
+    b.sms = ctx.sms;
+    return fp_mode() == FPSGPU_FP_FMA ? run_batch_fma((int)dim, b) : run_batch_nofma((int)dim, b);
+}
+
+int fpsgpu_kdline_batch(const float* raw_data, const size_t* offsets, size_t n_clouds, size_t dim,
+                        const size_t* n_samples, const size_t* start_idx, const size_t* height,
+                        size_t* sampled_point_indices) {
+    clear_error();
+    if (n_clouds == 0) return FPSGPU_OK;
+    if (!offsets || !n_samples) return set_error(FPSGPU_ERR_ARG, "null argument");
+    DevCtx ctx;
+    int rc;
+    if ((rc = current_ctx(&ctx))) return rc;
+    Scratch sc(ctx.stream);
+    const size_t n = offsets[n_clouds];
+    size_t ktot = 0;
+    for (size_t c = 0; c < n_clouds; ++c) ktot += n_samples[c];
+    float* d_pts;
+    uint64_t* d_out;
+    if ((rc = sc.alloc(&d_pts, n * (dim ? dim : 1)))) return rc;
+    if ((rc = sc.alloc(&d_out, ktot))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_pts, raw_data, n * dim * sizeof(float),
+                                    cudaMemcpyHostToDevice, ctx.stream));
+    if ((rc = fpsgpu_kdline_batch_device(d_pts, offsets, n_clouds, dim, n_samples, start_idx,
+                                         height, d_out, ctx.stream)))
+        return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(sampled_point_indices, d_out, ktot * sizeof(uint64_t),
                                     cudaMemcpyDeviceToHost, ctx.stream));
     FPSGPU_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
     return FPSGPU_OK;

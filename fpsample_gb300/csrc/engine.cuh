@@ -119,33 +119,28 @@ __device__ __forceinline__ float serial_sum(float acc, const float* buf, uint32_
     return acc;
 }
 
-// row-major points -> SoA, tag = original index, flags cleared, root node.
+// row-major points -> SoA, tag = original index; one root per cloud:
+// roots[c] = {first, end, 0, height}.  The flag array is zeroed beforehand.
 template <int D>
-__global__ void build_prepare(const float* __restrict__ pts, BuildArgs a, uint32_t height,
-                              int exact) {
+__global__ void build_prepare(const float* __restrict__ pts, BuildArgs a, const uint4* roots,
+                              uint32_t n_clouds, int exact) {
     const uint64_t n = a.n;
-    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n;
-         p += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t p = tid; p < n; p += stride) {
 #pragma unroll
         for (int d = 0; d < D; ++d) a.X[(uint64_t)d * n + p] = pts[p * D + d];
         a.tag[p] = (uint32_t)p;
-        a.flag[p] = 0;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        const uint4 root = make_uint4(0u, (uint32_t)n, 0u, height);
-        const bool root_leaf = !exact || height == 0 || n == 1;
-        if (root_leaf) {
-            *a.cnt_cur = 0;
-            if (n > kPiece) {
-                a.refine[0] = root;
-                *a.refine_cnt = 1;
-            } else {
-                *a.refine_cnt = 0;  // one piece; position 0 always starts one
-            }
-        } else {
-            a.cur[0] = root;
-            *a.cnt_cur = 1;
-            *a.refine_cnt = 0;
+    for (uint64_t c = tid; c < n_clouds; c += stride) {
+        const uint4 root = roots[c];
+        const uint32_t len = root.y - root.x;
+        if (len == 0) continue;
+        a.flag[root.x] = 1;  // every cloud starts a piece
+        if (exact && root.w > 0 && len > 1) {
+            a.cur[atomicAdd(a.cnt_cur, 1u)] = root;
+        } else if (len > kPiece) {
+            a.refine[atomicAdd(a.refine_cnt, 1u)] = root;
         }
     }
 }
@@ -474,7 +469,9 @@ struct SampleArgs {
     float* dis;              // [n] running distance
     uint64_t n;
     const uint32_t* pstart;  // [np + 1]
-    const uint32_t* npieces;
+    const uint32_t* npieces; // device count, or null: np_fixed
+    uint32_t np_fixed;
+    uint64_t id_offset;      // subtracted from every output index
     const float* plo;        // [np][D]
     const float* phi;
     uint64_t* pkey;          // [np]
@@ -564,7 +561,7 @@ __global__ void __launch_bounds__(kSampleThreads, 1) fps_sample(SampleArgs a) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const int G = gridDim.x;
     const uint64_t n = a.n;
-    const uint32_t np = *a.npieces;
+    const uint32_t np = a.npieces ? *a.npieces : a.np_fixed;
     const uint32_t total_warps = (uint32_t)G * nwarps;
     const uint32_t pw = (np + total_warps - 1) / total_warps;
     const uint32_t gw = blockIdx.x * nwarps + warp;
@@ -575,7 +572,7 @@ __global__ void __launch_bounds__(kSampleThreads, 1) fps_sample(SampleArgs a) {
     if (tid < D) s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
     if (tid == 0) s_abort = 0;
     if (blockIdx.x == 0 && tid == 0 && a.k > 0) {
-        a.out[0] = KD ? a.idmap[tag0] : tag0;
+        a.out[0] = (KD ? a.idmap[tag0] : tag0) - a.id_offset;
         if (a.trace) a.trace[0] = KD ? FLT_MAX : INFINITY;
     }
     __syncthreads();
@@ -613,7 +610,7 @@ __global__ void __launch_bounds__(kSampleThreads, 1) fps_sample(SampleArgs a) {
             } else {
                 if (lane < D) s_ref[lane] = a.Xref[(uint64_t)lane * n + tg];
                 if (blockIdx.x == 0 && lane == 0) {
-                    a.out[t + 1] = KD ? a.idmap[tg] : tg;
+                    a.out[t + 1] = (KD ? a.idmap[tg] : tg) - a.id_offset;
                     if (a.trace) a.trace[t + 1] = forced ? INFINITY : key_dist(g);
                 }
             }
@@ -627,9 +624,424 @@ __global__ void __launch_bounds__(kSampleThreads, 1) fps_sample(SampleArgs a) {
     }
 }
 
+// ---- batched sampling: one CTA per cloud -------------------------------------
+//
+// A persistent grid pulls clouds from a queue (largest first).  The CTA keeps
+// its cloud's piece records in shared memory: max key, bounding box and the
+// coordinates of the max point.  One iteration is: every warp tests its pieces
+// against the reference point, recomputes the dirty ones from global memory,
+// and offers its best (key, piece); warp 0 picks the winner and reads the next
+// reference point from the winning piece's record.  Two __syncthreads per
+// sample, no cross-CTA communication, no global load for the winner.
+constexpr int kBatchThreads = 256;
+
+struct BatchArgs {
+    const float* X;             // SoA [D][n], storage order (all clouds)
+    const uint32_t* tag;
+    float* dis;
+    uint64_t n;
+    const uint32_t* pstart;     // global piece starts
+    const float* plo;           // [np][D]
+    const float* phi;
+    const uint32_t* cloud_piece;  // [C + 1]
+    const uint64_t* cloud_off;    // [C + 1]
+    const uint64_t* cloud_k;      // [C]
+    const uint64_t* cloud_tag0;   // [C] tag of the first sample
+    const uint64_t* out_off;      // [C]
+    const uint32_t* order;        // [n_items] clouds in processing order
+    uint32_t n_items;
+    const float* Xref;
+    const uint32_t* idmap;      // kd-line: original index by tag; vanilla: null
+    uint64_t* out;
+    unsigned int* queue;
+    unsigned long long* counters;
+    uint32_t cap;               // piece records that fit in shared memory
+};
+
+template <int D, bool FMA, bool KD>
+__global__ void __launch_bounds__(kBatchThreads) batch_sample(BatchArgs a) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    __shared__ uint64_t s_wkey[32];
+    __shared__ uint32_t s_wq[32];
+    __shared__ float s_ref[kMaxDim];
+    __shared__ uint32_t s_item;
+    const uint32_t cap = a.cap;
+    uint64_t* s_key = reinterpret_cast<uint64_t*>(s_dyn);
+    float* s_lo = reinterpret_cast<float*>(s_key + cap);  // [D][cap]
+    float* s_hi = s_lo + (size_t)D * cap;
+    float* s_mc = s_hi + (size_t)D * cap;                 // coordinates of each piece's max
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const uint64_t n = a.n;
+    const float init = KD ? FLT_MAX : INFINITY;
+    unsigned long long tested = 0, touched = 0;
+
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(a.queue, 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        if (item >= a.n_items) break;
+        const uint32_t c = a.order[item];
+        const uint32_t P0 = a.cloud_piece[c];
+        const uint32_t np = a.cloud_piece[c + 1] - P0;
+        const uint64_t K = a.cloud_k[c];
+        const uint64_t coff = a.cloud_off[c];
+        const uint64_t ooff = a.out_off[c];
+        for (uint32_t i = tid; i < np; i += blockDim.x) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                s_lo[(size_t)d * cap + i] = a.plo[(uint64_t)(P0 + i) * D + d];
+                s_hi[(size_t)d * cap + i] = a.phi[(uint64_t)(P0 + i) * D + d];
+            }
+        }
+        const uint32_t tag0 = (uint32_t)a.cloud_tag0[c];
+        if (tid < D) s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
+        if (tid == 0 && K > 0) a.out[ooff] = (KD ? a.idmap[tag0] : tag0) - coff;
+        __syncthreads();
+        const uint32_t pw = (np + nwarps - 1) / nwarps;
+        const uint32_t q0 = warp * pw < np ? warp * pw : np;
+        const uint32_t q1 = q0 + pw < np ? q0 + pw : np;
+
+        for (uint64_t t = 0; t + 1 < K; ++t) {
+            float r[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) r[d] = s_ref[d];
+            uint64_t best = 0;
+            uint32_t bestq = 0;
+            if (t > 0) tested += q1 - q0;
+            for (uint32_t qb = q0; qb < q1; qb += 32) {
+                const uint32_t q = qb + lane;
+                const bool have = q < q1;
+                uint64_t key = have && t > 0 ? s_key[q] : 0ull;
+                bool dirty = have;
+                if (have && t > 0) {
+                    float lo[D], hi[D];
+#pragma unroll
+                    for (int d = 0; d < D; ++d) {
+                        lo[d] = s_lo[(size_t)d * cap + q];
+                        hi[d] = s_hi[(size_t)d * cap + q];
+                    }
+                    dirty = box_bound<D, FMA>(lo, hi, r) < key_dist(key);
+                }
+                uint32_t m = __ballot_sync(kFull, dirty);
+                while (m) {
+                    const int l = __ffs(m) - 1;
+                    m &= m - 1;
+                    const uint32_t qq = qb + l;
+                    const uint32_t ps = __ldg(a.pstart + P0 + qq), pe = __ldg(a.pstart + P0 + qq + 1);
+                    touched += pe - ps;
+                    uint64_t pk = 0;
+                    float pc[D];
+#pragma unroll
+                    for (int d = 0; d < D; ++d) pc[d] = 0.0f;
+                    for (uint32_t p = ps + lane; p < pe; p += 32) {
+                        float x[D];
+#pragma unroll
+                        for (int d = 0; d < D; ++d) x[d] = __ldg(a.X + (uint64_t)d * n + p);
+                        float dv = t == 0 ? init : a.dis[p];
+                        const float dd = sqdist<D, FMA>(x, r);
+                        if (dd < dv) {
+                            dv = dd;
+                            if (t > 0) a.dis[p] = dv;
+                        }
+                        if (t == 0) a.dis[p] = dv;
+                        const uint64_t kk = make_key<KD>(dv, __ldg(a.tag + p));
+                        if (kk > pk) {
+                            pk = kk;
+#pragma unroll
+                            for (int d = 0; d < D; ++d) pc[d] = x[d];
+                        }
+                    }
+                    const uint64_t wk = warp_max_key(pk);
+                    const int owner = __ffs(__ballot_sync(kFull, pk == wk)) - 1;
+#pragma unroll
+                    for (int d = 0; d < D; ++d) pc[d] = __shfl_sync(kFull, pc[d], owner);
+                    if (lane == l) {
+                        key = wk;
+                        s_key[qq] = wk;
+#pragma unroll
+                        for (int d = 0; d < D; ++d) s_mc[(size_t)d * cap + qq] = pc[d];
+                    }
+                }
+                if (have && key > best) {
+                    best = key;
+                    bestq = q;
+                }
+            }
+            const uint64_t wb = warp_max_key(best);
+            const int wl = __ffs(__ballot_sync(kFull, best == wb)) - 1;
+            bestq = __shfl_sync(kFull, bestq, wl);
+            if (lane == 0) {
+                s_wkey[warp] = wb;
+                s_wq[warp] = bestq;
+            }
+            __syncthreads();
+            if (warp == 0) {
+                const uint64_t kw = lane < nwarps ? s_wkey[lane] : 0ull;
+                const uint64_t g = warp_max_key(kw);
+                const int w = __ffs(__ballot_sync(kFull, lane < nwarps && kw == g)) - 1;
+                const uint32_t qwin = s_wq[w];
+                if (lane < D) s_ref[lane] = s_mc[(size_t)lane * cap + qwin];
+                if (lane == 0) {
+                    const uint32_t tg = key_pos<KD>(g);
+                    a.out[ooff + t + 1] = (KD ? a.idmap[tg] : tg) - coff;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (a.counters && lane == 0) {
+        atomicAdd(a.counters, tested);
+        atomicAdd(a.counters + 1, touched);
+    }
+}
+
+// first piece of every cloud: lower bound of cloud_off[c] in pstart[0, np]
+__global__ void cloud_piece_ranges(const uint32_t* pstart, const uint32_t* npieces,
+                                   const uint64_t* cloud_off, uint32_t n_clouds, uint32_t* out);
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+
+// A set of clouds stored back to back: cloud c holds positions
+// [off[c], off[c+1]) of the row-major point buffer.
+struct CloudSet {
+    const float* d_points;
+    std::vector<uint64_t> off;     // C + 1
+    std::vector<uint64_t> height;  // kd-line tree height per cloud
+    bool kd = true;
+};
+
+// Device arrays produced by build_clouds.
+struct Built {
+    float* X = nullptr;
+    uint32_t* tag = nullptr;
+    float* Xref = nullptr;
+    uint32_t* idsnap = nullptr;
+    uint8_t* flag = nullptr;
+    uint4* refine = nullptr;
+    uint32_t* refine_cnt = nullptr;
+    uint32_t* pstart = nullptr;
+    uint32_t* d_np = nullptr;
+    float* plo = nullptr;
+    float* phi = nullptr;
+    uint64_t np_cap = 0;
+    int* err = nullptr;
+};
+
+// Exact kd-line levels (kd), snapshot, refinement, pieces and their boxes for
+// every cloud of the set.  build_only stops after the snapshot.
+template <int D>
+int build_clouds(const CloudSet& cs, cudaStream_t stream, Scratch& sc, Built& out,
+                 bool build_only) {
+    const size_t C = cs.off.size() - 1;
+    const uint64_t n = cs.off[C];
+    int rc;
+    BuildArgs b{};
+    b.n = n;
+    if ((rc = sc.alloc(&b.X, n * D))) return rc;
+    if ((rc = sc.alloc(&b.tag, n))) return rc;
+    if ((rc = sc.alloc(&b.sel, n))) return rc;
+    if ((rc = sc.alloc(&b.flag, n))) return rc;
+    if ((rc = sc.alloc(&b.err, 1))) return rc;
+    const uint64_t node_cap = n / 2 + C + 1;
+    uint4 *list_a, *list_b;
+    if ((rc = sc.alloc(&list_a, node_cap))) return rc;
+    if ((rc = sc.alloc(&list_b, node_cap))) return rc;
+    const uint64_t rcap = n / (kPiece + 1) + 2;
+    if ((rc = sc.alloc(&b.refine, rcap))) return rc;
+
+    // per-cloud exact depth and host-side bounds on node counts
+    uint64_t levels = 0, max_n = 1;
+    std::vector<uint64_t> lv(C);
+    std::vector<uint4> h_roots(C);
+    for (size_t c = 0; c < C; ++c) {
+        const uint64_t nc = cs.off[c + 1] - cs.off[c];
+        lv[c] = cs.kd && nc > 0 ? std::min<uint64_t>(cs.height[c], nc - 1) : 0;
+        levels = std::max(levels, lv[c]);
+        max_n = std::max(max_n, nc);
+        h_roots[c] = make_uint4((uint32_t)cs.off[c], (uint32_t)cs.off[c + 1], 0u,
+                                (uint32_t)std::min<uint64_t>(cs.height[c], 0xffffffffull));
+    }
+    const int refine_levels = 10 + (int)std::ceil(std::log2((double)max_n / kPiece + 1.0));
+    const uint64_t ncounters = 1 + (levels + 1) + (refine_levels + 1);
+    uint32_t* counters;
+    if ((rc = sc.alloc(&counters, ncounters))) return rc;
+    uint4* d_roots;
+    if ((rc = sc.alloc(&d_roots, C))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemsetAsync(counters, 0, ncounters * sizeof(uint32_t), stream));
+    FPSGPU_CUDA_TRY(cudaMemsetAsync(b.err, 0, sizeof(int), stream));
+    FPSGPU_CUDA_TRY(cudaMemsetAsync(b.flag, 0, n, stream));
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_roots, h_roots.data(), C * sizeof(uint4),
+                                    cudaMemcpyHostToDevice, stream));
+    b.refine_cnt = counters;
+    uint32_t* level_cnt = counters + 1;
+
+    const unsigned elem_blocks = (unsigned)std::min<uint64_t>((n + 255) / 256 + 1, 8192);
+    b.cur = list_a;
+    b.next = list_b;
+    b.cnt_cur = level_cnt;
+    stats_count_launch();
+    build_prepare<D><<<elem_blocks, 256, 0, stream>>>(cs.d_points, b, d_roots, (uint32_t)C,
+                                                      cs.kd ? 1 : 0);
+    FPSGPU_CUDA_TRY(cudaGetLastError());
+
+    // exact phase: one launch per level; grid = bound on that level's nodes
+    for (uint64_t j = 0; j < levels; ++j) {
+        uint64_t bound = 0;
+        for (size_t c = 0; c < C; ++c) {
+            if (j >= lv[c]) continue;
+            const uint64_t nc = cs.off[c + 1] - cs.off[c];
+            bound += std::min<uint64_t>(j < 40 ? (1ull << j) : nc, nc / 2 + 1);
+        }
+        bound = std::min<uint64_t>(bound, node_cap);
+        if (bound > 65536) {  // read the exact count instead of launching empty CTAs
+            uint32_t h_cnt = 0;
+            FPSGPU_CUDA_TRY(cudaMemcpyAsync(&h_cnt, level_cnt + j, sizeof(uint32_t),
+                                            cudaMemcpyDeviceToHost, stream));
+            FPSGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+            bound = h_cnt;
+        }
+        if (bound == 0) break;
+        b.cnt_cur = level_cnt + j;
+        b.cnt_next = level_cnt + j + 1;
+        stats_count_launch();
+        split_kernel<D, true><<<(unsigned)bound, kBuildThreads, 0, stream>>>(b, 0);
+        FPSGPU_CUDA_TRY(cudaGetLastError());
+        std::swap(b.cur, b.next);
+    }
+
+    if ((rc = sc.alloc(&out.Xref, n * D))) return rc;
+    if (cs.kd && (rc = sc.alloc(&out.idsnap, n))) return rc;
+    stats_count_launch();
+    build_snapshot<D><<<elem_blocks, 256, 0, stream>>>(b, out.Xref, out.idsnap);
+    FPSGPU_CUDA_TRY(cudaGetLastError());
+    out.X = b.X;
+    out.tag = b.tag;
+    out.flag = b.flag;
+    out.refine = b.refine;
+    out.refine_cnt = b.refine_cnt;
+    out.err = b.err;
+    if (build_only) return FPSGPU_OK;
+
+    // refinement phase
+    uint32_t* rcnt = level_cnt + levels + 1;
+    b.cnt_cur = rcnt;
+    stats_count_launch();
+    build_seed_refine<<<64, 256, 0, stream>>>(b);
+    FPSGPU_CUDA_TRY(cudaGetLastError());
+    uint64_t rbound = 0, nb_bound = 0;
+    for (size_t c = 0; c < C; ++c) {
+        const uint64_t nc = cs.off[c + 1] - cs.off[c];
+        const uint64_t leaves = lv[c] < 40 ? std::min<uint64_t>(1ull << lv[c], nc) : nc;
+        nb_bound += leaves;
+        rbound += std::min<uint64_t>(leaves, nc / (kPiece + 1) + 1);
+    }
+    rbound = std::min<uint64_t>(rbound, rcap);
+    for (int j = 0; j < refine_levels && rbound > 0; ++j) {
+        b.cnt_cur = rcnt + j;
+        b.cnt_next = rcnt + j + 1;
+        const int last = j + 1 == refine_levels;
+        stats_count_launch();
+        split_kernel<D, false><<<(unsigned)rbound, kRefineThreads, 0, stream>>>(b, last);
+        FPSGPU_CUDA_TRY(cudaGetLastError());
+        std::swap(b.cur, b.next);
+        rbound = std::min<uint64_t>(2 * rbound, rcap);
+    }
+
+    // pieces: exact leaves of <= kPiece points, two children per refined node
+    // on every refinement level, everything left on the last one
+    const uint64_t per_level = n / (kPiece + 1) + 1;
+    out.np_cap = std::min<uint64_t>(n, nb_bound + (2ull * refine_levels + 1) * per_level + C + 1);
+    if ((rc = sc.alloc(&out.pstart, out.np_cap + 1))) return rc;
+    if ((rc = sc.alloc(&out.d_np, 1))) return rc;
+    if ((rc = compact_flags(b.flag, n, out.pstart, out.d_np, sc, stream))) return rc;
+    if ((rc = sc.alloc(&out.plo, out.np_cap * D))) return rc;
+    if ((rc = sc.alloc(&out.phi, out.np_cap * D))) return rc;
+    {
+        const unsigned blocks = (unsigned)std::min<uint64_t>((out.np_cap * 32 + 255) / 256, 4096);
+        stats_count_launch();
+        piece_bbox<D><<<blocks, 256, 0, stream>>>(b.X, n, out.pstart, out.d_np, out.plo, out.phi);
+        FPSGPU_CUDA_TRY(cudaGetLastError());
+    }
+    return FPSGPU_OK;
+}
+
+inline int check_device_error(const int* d_err, cudaStream_t stream) {
+    int h_err = 0;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    FPSGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (h_err & kErrNonFiniteSplit)
+        return set_error(FPSGPU_ERR_NONFINITE,
+                         "kd-line build met a NaN coordinate in a split dimension");
+    if (h_err)
+        return set_error(FPSGPU_ERR_DEVICE, "FPS sampler gave up (device error word 0x%x)", h_err);
+    return FPSGPU_OK;
+}
+
+// Multi-CTA sampler over pieces [piece0, piece0 + np) (np == ~0u: the device
+// count of the whole build).
+template <int D, bool FMA>
+int sample_grid(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint32_t np,
+                uint64_t points_in_range, uint64_t k, const uint64_t* h_forced, uint32_t n_forced,
+                uint64_t id_offset, uint64_t* d_out, float* d_trace, cudaStream_t stream, int sms,
+                Scratch& sc) {
+    int rc;
+    float* dis;
+    uint64_t* pkey;
+    const uint64_t nkeys = np == ~0u ? bt.np_cap : np;
+    if ((rc = sc.alloc(&dis, n))) return rc;
+    if ((rc = sc.alloc(&pkey, nkeys))) return rc;
+    // grid: about two pieces per warp (pieces hold ~kPiece/2..kPiece points)
+    uint64_t G = (points_in_range / (kPiece / 2) + 63) / 64;
+    G = std::max<uint64_t>(1, std::min<uint64_t>(G, (uint64_t)sms));
+    uint64_t* slots;
+    if ((rc = sc.alloc(&slots, 3 * G))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemsetAsync(slots, 0, 3 * G * sizeof(uint64_t), stream));
+    uint64_t* d_forced;
+    if ((rc = sc.alloc(&d_forced, n_forced))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_forced, h_forced, n_forced * sizeof(uint64_t),
+                                    cudaMemcpyHostToDevice, stream));
+    unsigned long long* cnt;
+    if ((rc = sc.alloc(&cnt, 2))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), stream));
+
+    SampleArgs s{};
+    s.X = bt.X;
+    s.tag = bt.tag;
+    s.dis = dis;
+    s.n = n;
+    s.pstart = bt.pstart + piece0;
+    s.npieces = np == ~0u ? bt.d_np : nullptr;
+    s.np_fixed = np == ~0u ? 0 : np;
+    s.id_offset = id_offset;
+    s.plo = bt.plo + (uint64_t)piece0 * D;
+    s.phi = bt.phi + (uint64_t)piece0 * D;
+    s.pkey = pkey;
+    s.Xref = bt.Xref;
+    s.idmap = bt.idsnap;
+    s.k = k;
+    s.forced = d_forced;
+    s.n_forced = n_forced;
+    s.out = d_out;
+    s.trace = d_trace;
+    s.slots = slots;
+    s.err = bt.err;
+    s.counters = cnt;
+    void* args[] = {&s};
+    SamplerTimer timer;
+    timer.begin(stream);
+    const void* kern = kd ? (const void*)fps_sample<D, FMA, true> : (const void*)fps_sample<D, FMA, false>;
+    if ((rc = launch_persistent(kern, (int)G, kSampleThreads, args, 0, stream, G > 1))) return rc;
+    timer.end(stream);
+    unsigned long long h_cnt[2] = {0, 0};
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, stream));
+    if ((rc = check_device_error(bt.err, stream))) return rc;
+    const uint64_t cn[2] = {h_cnt[0], h_cnt[1]};
+    timer.finish(k, cn);
+    return FPSGPU_OK;
+}
+
 struct EngineCall {
     const float* d_points;  // row-major [n][D]
     uint64_t n;
@@ -651,92 +1063,32 @@ struct EngineCall {
 template <int D, bool FMA>
 int run_engine(const EngineCall& c) {
     Scratch sc(c.stream);
-    const uint64_t n = c.n;
+    CloudSet cs;
+    cs.d_points = c.d_points;
+    cs.off = {0, c.n};
+    cs.height = {c.height};
+    cs.kd = c.kd;
+    Built bt;
     int rc;
-    BuildArgs b{};
-    b.n = n;
-    if ((rc = sc.alloc(&b.X, n * D))) return rc;
-    if ((rc = sc.alloc(&b.tag, n))) return rc;
-    if ((rc = sc.alloc(&b.sel, n))) return rc;
-    if ((rc = sc.alloc(&b.flag, n))) return rc;
-    if ((rc = sc.alloc(&b.err, 1))) return rc;
-    const uint64_t node_cap = n / 2 + 1;
-    uint4 *list_a, *list_b;
-    if ((rc = sc.alloc(&list_a, node_cap))) return rc;
-    if ((rc = sc.alloc(&list_b, node_cap))) return rc;
-    if ((rc = sc.alloc(&b.refine, n / (kPiece + 1) + 2))) return rc;
-    // counters: [0] refine count, then one per level (exact + refinement)
-    const uint64_t levels = c.kd ? (c.height < n - 1 ? c.height : n - 1) : 0;
-    const int refine_levels = 10 + (int)std::ceil(std::log2((double)n / kPiece + 1.0));
-    const uint64_t ncounters = 1 + levels + 1 + refine_levels + 1;
-    uint32_t* counters;
-    if ((rc = sc.alloc(&counters, ncounters))) return rc;
-    FPSGPU_CUDA_TRY(cudaMemsetAsync(counters, 0, ncounters * sizeof(uint32_t), c.stream));
-    FPSGPU_CUDA_TRY(cudaMemsetAsync(b.err, 0, sizeof(int), c.stream));
-    b.refine_cnt = counters;
-    uint32_t* level_cnt = counters + 1;
-
-    const unsigned elem_blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 8192);
-    b.cur = list_a;
-    b.next = list_b;
-    b.cnt_cur = level_cnt;
-    stats_count_launch();
-    build_prepare<D><<<elem_blocks, 256, 0, c.stream>>>(c.d_points, b, (uint32_t)c.height,
-                                                         c.kd ? 1 : 0);
-    FPSGPU_CUDA_TRY(cudaGetLastError());
-
-    // exact phase (kd-line): one launch per level, grid = a bound on the nodes
-    uint64_t bound = levels == 0 ? 0 : 1;
-    uint32_t* cnt = level_cnt;
-    for (uint64_t j = 0; j < levels && bound > 0; ++j) {
-        b.cnt_cur = cnt;
-        b.cnt_next = cnt + 1;
-        stats_count_launch();
-        split_kernel<D, true><<<(unsigned)bound, kBuildThreads, 0, c.stream>>>(b, 0);
-        FPSGPU_CUDA_TRY(cudaGetLastError());
-        std::swap(b.cur, b.next);
-        ++cnt;
-        bound = std::min<uint64_t>(2 * bound, node_cap);
-        if (bound > 65536) {  // read the exact count instead of launching empty CTAs
-            uint32_t h_cnt = 0;
-            FPSGPU_CUDA_TRY(cudaMemcpyAsync(&h_cnt, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                                            c.stream));
-            FPSGPU_CUDA_TRY(cudaStreamSynchronize(c.stream));
-            bound = h_cnt;
-        }
-    }
-    // In the exact phase nodes that reach the last level without becoming
-    // leaves cannot exist: depth == height makes every child a leaf.
-
-    float* Xref;
-    uint32_t* idsnap = nullptr;
-    if ((rc = sc.alloc(&Xref, n * D))) return rc;
-    if (c.kd && (rc = sc.alloc(&idsnap, n))) return rc;
-    stats_count_launch();
-    build_snapshot<D><<<elem_blocks, 256, 0, c.stream>>>(b, Xref, idsnap);
-    FPSGPU_CUDA_TRY(cudaGetLastError());
+    if ((rc = build_clouds<D>(cs, c.stream, sc, bt, c.h_perm != nullptr))) return rc;
+    const uint64_t n = c.n;
 
     if (c.h_perm) {  // build-only: reference permutation and buckets
         std::vector<uint32_t> h_id(n);
-        int h_err = 0;
         uint32_t h_nref = 0;
-        FPSGPU_CUDA_TRY(cudaMemcpyAsync(h_id.data(), idsnap ? idsnap : b.tag, n * sizeof(uint32_t),
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(h_id.data(), bt.idsnap, n * sizeof(uint32_t),
                                         cudaMemcpyDeviceToHost, c.stream));
-        FPSGPU_CUDA_TRY(cudaMemcpyAsync(&h_err, b.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-        FPSGPU_CUDA_TRY(cudaMemcpyAsync(&h_nref, b.refine_cnt, sizeof(uint32_t),
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(&h_nref, bt.refine_cnt, sizeof(uint32_t),
                                         cudaMemcpyDeviceToHost, c.stream));
-        FPSGPU_CUDA_TRY(cudaStreamSynchronize(c.stream));
-        if (h_err & kErrNonFiniteSplit)
-            return set_error(FPSGPU_ERR_NONFINITE,
-                             "kd-line build met a NaN coordinate in a split dimension");
+        if ((rc = check_device_error(bt.err, c.stream))) return rc;
         // buckets = exact leaves: the ones queued for refinement plus the small
         // ones already flagged as pieces
         std::vector<uint4> h_ref(h_nref);
         std::vector<uint8_t> h_flag(n);
         if (h_nref)
-            FPSGPU_CUDA_TRY(cudaMemcpy(h_ref.data(), b.refine, h_nref * sizeof(uint4),
+            FPSGPU_CUDA_TRY(cudaMemcpy(h_ref.data(), bt.refine, h_nref * sizeof(uint4),
                                        cudaMemcpyDeviceToHost));
-        FPSGPU_CUDA_TRY(cudaMemcpy(h_flag.data(), b.flag, n, cudaMemcpyDeviceToHost));
+        FPSGPU_CUDA_TRY(cudaMemcpy(h_flag.data(), bt.flag, n, cudaMemcpyDeviceToHost));
         for (const uint4& r : h_ref) h_flag[r.x] = 1;
         h_flag[0] = 1;
         size_t nb = 0;
@@ -746,108 +1098,152 @@ int run_engine(const EngineCall& c) {
         *c.h_n_buckets = nb;
         return FPSGPU_OK;
     }
+    return sample_grid<D, FMA>(bt, n, c.kd, 0, ~0u, n, c.k, c.h_forced, c.n_forced, 0, c.d_out,
+                               c.d_trace, c.stream, c.sms, sc);
+}
 
-    // refinement phase
-    {
-        uint32_t* rcnt = level_cnt + levels + 1;
-        b.cnt_cur = rcnt;
-        stats_count_launch();
-        build_seed_refine<<<64, 256, 0, c.stream>>>(b);  // refine list -> b.cur, *rcnt
-        FPSGPU_CUDA_TRY(cudaGetLastError());
-        uint64_t rbound = c.kd ? std::min<uint64_t>(levels < 40 ? (1ull << levels) : n,
-                                                    n / (kPiece + 1) + 1)
-                               : 1;
-        const uint64_t rcap = n / (kPiece + 1) + 2;
-        for (int j = 0; j < refine_levels && rbound > 0; ++j) {
-            b.cnt_cur = rcnt + j;
-            b.cnt_next = rcnt + j + 1;
-            const int last = j + 1 == refine_levels;
-            stats_count_launch();
-            split_kernel<D, false><<<(unsigned)rbound, kRefineThreads, 0, c.stream>>>(b, last);
-            FPSGPU_CUDA_TRY(cudaGetLastError());
-            std::swap(b.cur, b.next);
-            rbound = std::min<uint64_t>(2 * rbound, rcap);
+// Many clouds in one go: build all of them together, then one CTA per cloud
+// (clouds whose piece records do not fit in shared memory use sample_grid).
+struct BatchCall {
+    const float* d_points;            // all clouds, row-major, back to back
+    std::vector<uint64_t> off;        // C + 1
+    std::vector<uint64_t> k;          // C
+    std::vector<uint64_t> start;      // C (local start index / position)
+    std::vector<uint64_t> height;     // C
+    bool kd;
+    uint64_t* d_out;                  // sum(k), cloud c at out_off[c]
+    cudaStream_t stream;
+    int sms;
+};
+
+constexpr size_t kBatchSmemMax = 100 * 1024;
+
+template <int D, bool FMA>
+int run_batch(const BatchCall& bc) {
+    Scratch sc(bc.stream);
+    const size_t C = bc.off.size() - 1;
+    const uint64_t n = bc.off[C];
+    int rc;
+    CloudSet cs;
+    cs.d_points = bc.d_points;
+    cs.off = bc.off;
+    cs.height = bc.height;
+    cs.kd = bc.kd;
+    Built bt;
+    if ((rc = build_clouds<D>(cs, bc.stream, sc, bt, false))) return rc;
+
+    uint64_t* d_coff;
+    uint32_t* d_cpiece;
+    if ((rc = sc.alloc(&d_coff, C + 1))) return rc;
+    if ((rc = sc.alloc(&d_cpiece, C + 1))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_coff, bc.off.data(), (C + 1) * sizeof(uint64_t),
+                                    cudaMemcpyHostToDevice, bc.stream));
+    stats_count_launch();
+    cloud_piece_ranges<<<(unsigned)((C + 1 + 255) / 256), 256, 0, bc.stream>>>(
+        bt.pstart, bt.d_np, d_coff, (uint32_t)C, d_cpiece);
+    FPSGPU_CUDA_TRY(cudaGetLastError());
+    std::vector<uint32_t> h_cpiece(C + 1);
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(h_cpiece.data(), d_cpiece, (C + 1) * sizeof(uint32_t),
+                                    cudaMemcpyDeviceToHost, bc.stream));
+    if ((rc = check_device_error(bt.err, bc.stream))) return rc;
+
+    const size_t rec = sizeof(uint64_t) + 3 * D * sizeof(float);
+    const uint32_t cap_max = (uint32_t)(kBatchSmemMax / rec);
+    std::vector<uint64_t> out_off(C), tag0(C);
+    std::vector<uint32_t> small, big;
+    uint64_t acc = 0;
+    uint32_t cap = 1;
+    for (size_t c = 0; c < C; ++c) {
+        out_off[c] = acc;
+        acc += bc.k[c];
+        // kd-line: the start is a position of the cloud's permuted order, i.e.
+        // a tag; vanilla: the start is an original index, also a tag
+        tag0[c] = bc.off[c] + bc.start[c];
+        const uint32_t np = h_cpiece[c + 1] - h_cpiece[c];
+        if (bc.k[c] == 0) continue;
+        if (np <= cap_max) {
+            small.push_back((uint32_t)c);
+            cap = std::max(cap, np);
+        } else {
+            big.push_back((uint32_t)c);
         }
     }
+    // largest first
+    std::sort(small.begin(), small.end(), [&](uint32_t x, uint32_t y) {
+        return bc.k[x] * (bc.off[x + 1] - bc.off[x]) > bc.k[y] * (bc.off[y + 1] - bc.off[y]);
+    });
 
-    // pieces
-    // pieces: exact leaves of <= kPiece points (<= 2^levels), two children per
-    // refined node on every refinement level, everything left on the last one
-    const uint64_t per_level = n / (kPiece + 1) + 1;
-    const uint64_t np_cap = std::min<uint64_t>(
-        n, (levels < 40 ? (1ull << levels) : n) + (2ull * refine_levels + 1) * per_level + 1);
-    uint32_t* pstart;
-    uint32_t* d_np;
-    if ((rc = sc.alloc(&pstart, np_cap + 1))) return rc;
-    if ((rc = sc.alloc(&d_np, 1))) return rc;
-    if ((rc = compact_flags(b.flag, n, pstart, d_np, sc, c.stream))) return rc;
-    float *plo, *phi, *dis;
-    uint64_t* pkey;
-    if ((rc = sc.alloc(&plo, np_cap * D))) return rc;
-    if ((rc = sc.alloc(&phi, np_cap * D))) return rc;
-    if ((rc = sc.alloc(&pkey, np_cap))) return rc;
-    if ((rc = sc.alloc(&dis, n))) return rc;
-    {
-        const unsigned blocks = (unsigned)std::min<uint64_t>((np_cap * 32 + 255) / 256, 4096);
-        stats_count_launch();
-        piece_bbox<D><<<blocks, 256, 0, c.stream>>>(b.X, n, pstart, d_np, plo, phi);
-        FPSGPU_CUDA_TRY(cudaGetLastError());
-    }
-    // grid: about two pieces per warp (pieces hold ~kPiece/2..kPiece points)
-    uint64_t G = (n / (kPiece / 2) + 63) / 64;
-    G = std::max<uint64_t>(1, std::min<uint64_t>(G, (uint64_t)c.sms));
-    uint64_t* slots;
-    if ((rc = sc.alloc(&slots, 3 * G))) return rc;
-    FPSGPU_CUDA_TRY(cudaMemsetAsync(slots, 0, 3 * G * sizeof(uint64_t), c.stream));
-    uint64_t* d_forced;
-    if ((rc = sc.alloc(&d_forced, c.n_forced))) return rc;
-    FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_forced, c.h_forced, c.n_forced * sizeof(uint64_t),
-                                    cudaMemcpyHostToDevice, c.stream));
-    unsigned long long* sc_counters;
-    if ((rc = sc.alloc(&sc_counters, 2))) return rc;
-    FPSGPU_CUDA_TRY(cudaMemsetAsync(sc_counters, 0, 2 * sizeof(unsigned long long), c.stream));
-
-    SampleArgs s{};
-    s.X = b.X;
-    s.tag = b.tag;
-    s.dis = dis;
-    s.n = n;
-    s.pstart = pstart;
-    s.npieces = d_np;
-    s.plo = plo;
-    s.phi = phi;
-    s.pkey = pkey;
-    s.Xref = Xref;
-    s.idmap = idsnap;
-    s.k = c.k;
-    s.forced = d_forced;
-    s.n_forced = c.n_forced;
-    s.out = c.d_out;
-    s.trace = c.d_trace;
-    s.slots = slots;
-    s.err = b.err;
-    s.counters = sc_counters;
-    void* args[] = {&s};
-    SamplerTimer timer;
-    timer.begin(c.stream);
-    const void* kern = c.kd ? (const void*)fps_sample<D, FMA, true> : (const void*)fps_sample<D, FMA, false>;
-    if ((rc = launch_persistent(kern, (int)G, kSampleThreads, args, 0, c.stream, G > 1))) return rc;
-    timer.end(c.stream);
-    int h_err = 0;
-    unsigned long long h_cnt[2] = {0, 0};
-    FPSGPU_CUDA_TRY(cudaMemcpyAsync(&h_err, b.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-    FPSGPU_CUDA_TRY(cudaMemcpyAsync(h_cnt, sc_counters, sizeof(h_cnt), cudaMemcpyDeviceToHost, c.stream));
-    FPSGPU_CUDA_TRY(cudaStreamSynchronize(c.stream));
-    {
+    if (!small.empty()) {
+        uint64_t *d_k, *d_tag0, *d_ooff;
+        uint32_t* d_order;
+        unsigned int* d_queue;
+        unsigned long long* cnt;
+        float* dis;
+        if ((rc = sc.alloc(&d_k, C))) return rc;
+        if ((rc = sc.alloc(&d_tag0, C))) return rc;
+        if ((rc = sc.alloc(&d_ooff, C))) return rc;
+        if ((rc = sc.alloc(&d_order, small.size()))) return rc;
+        if ((rc = sc.alloc(&d_queue, 1))) return rc;
+        if ((rc = sc.alloc(&cnt, 2))) return rc;
+        if ((rc = sc.alloc(&dis, n))) return rc;
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_k, bc.k.data(), C * 8, cudaMemcpyHostToDevice, bc.stream));
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_tag0, tag0.data(), C * 8, cudaMemcpyHostToDevice, bc.stream));
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_ooff, out_off.data(), C * 8, cudaMemcpyHostToDevice, bc.stream));
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_order, small.data(), small.size() * 4,
+                                        cudaMemcpyHostToDevice, bc.stream));
+        FPSGPU_CUDA_TRY(cudaMemsetAsync(d_queue, 0, sizeof(unsigned int), bc.stream));
+        FPSGPU_CUDA_TRY(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), bc.stream));
+        BatchArgs a{};
+        a.X = bt.X;
+        a.tag = bt.tag;
+        a.dis = dis;
+        a.n = n;
+        a.pstart = bt.pstart;
+        a.plo = bt.plo;
+        a.phi = bt.phi;
+        a.cloud_piece = d_cpiece;
+        a.cloud_off = d_coff;
+        a.cloud_k = d_k;
+        a.cloud_tag0 = d_tag0;
+        a.out_off = d_ooff;
+        a.order = d_order;
+        a.n_items = (uint32_t)small.size();
+        a.Xref = bt.Xref;
+        a.idmap = bt.idsnap;
+        a.out = bc.d_out;
+        a.queue = d_queue;
+        a.counters = cnt;
+        a.cap = cap;
+        const size_t smem = (size_t)cap * rec;
+        const void* kern = bc.kd ? (const void*)batch_sample<D, FMA, true>
+                                 : (const void*)batch_sample<D, FMA, false>;
+        FPSGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem));
+        int per_sm = 0;
+        FPSGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBatchThreads, smem));
+        const int G = (int)std::min<uint64_t>(small.size(), (uint64_t)std::max(1, per_sm) * bc.sms);
+        void* args[] = {&a};
+        SamplerTimer timer;
+        timer.begin(bc.stream);
+        if ((rc = launch_persistent(kern, G, kBatchThreads, args, smem, bc.stream, false))) return rc;
+        timer.end(bc.stream);
+        unsigned long long h_cnt[2] = {0, 0};
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, bc.stream));
+        FPSGPU_CUDA_TRY(cudaStreamSynchronize(bc.stream));
+        uint64_t ks = 0;
+        for (uint32_t c : small) ks += bc.k[c];
         const uint64_t cn[2] = {h_cnt[0], h_cnt[1]};
-        timer.finish(c.k, cn);
+        timer.finish(ks, cn);
     }
-    if (h_err & kErrNonFiniteSplit)
-        return set_error(FPSGPU_ERR_NONFINITE,
-                         "kd-line build met a NaN coordinate in a split dimension");
-    if (h_err)
-        return set_error(FPSGPU_ERR_DEVICE, "FPS sampler gave up (device error word 0x%x)", h_err);
-    return FPSGPU_OK;
+    for (uint32_t c : big) {
+        const uint64_t f = tag0[c];
+        const uint32_t np = h_cpiece[c + 1] - h_cpiece[c];
+        if ((rc = sample_grid<D, FMA>(bt, n, bc.kd, h_cpiece[c], np, bc.off[c + 1] - bc.off[c],
+                                      bc.k[c], &f, 1, bc.off[c], bc.d_out + out_off[c], nullptr,
+                                      bc.stream, bc.sms, sc)))
+            return rc;
+    }
+    return check_device_error(bt.err, bc.stream);
 }
 
 template <bool FMA>
@@ -861,6 +1257,21 @@ int run_engine_dispatch(int dim, const EngineCall& c) {
         case 6: return run_engine<6, FMA>(c);
         case 7: return run_engine<7, FMA>(c);
         case 8: return run_engine<8, FMA>(c);
+        default: return set_error(FPSGPU_ERR_DIM, "dim must be in [1, 8], got %d", dim);
+    }
+}
+
+template <bool FMA>
+int run_batch_dispatch(int dim, const BatchCall& c) {
+    switch (dim) {
+        case 1: return run_batch<1, FMA>(c);
+        case 2: return run_batch<2, FMA>(c);
+        case 3: return run_batch<3, FMA>(c);
+        case 4: return run_batch<4, FMA>(c);
+        case 5: return run_batch<5, FMA>(c);
+        case 6: return run_batch<6, FMA>(c);
+        case 7: return run_batch<7, FMA>(c);
+        case 8: return run_batch<8, FMA>(c);
         default: return set_error(FPSGPU_ERR_DIM, "dim must be in [1, 8], got %d", dim);
     }
 }

@@ -119,42 +119,64 @@ __device__ __forceinline__ int ld_relaxed_gpu_s32(const int* p) {
     return v;
 }
 
+__device__ __forceinline__ uint64_t ld_relaxed_gpu(const uint64_t* p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+// Largest grid exchange_max supports (slots polled per lane: kMaxGrid / 32).
+constexpr int kMaxGrid = 256;
+
 // Cross-CTA argmax for persistent kernels whose CTAs are all co-resident
 // (cooperative launch).  Called by ONE full warp per CTA, once per round.
 //
 // slots: 3 * G u64, zeroed before the launch.  Round t uses row t % 3.  Every
 // CTA publishes its key (never 0: bit 63 is set) with a release store, then
-// polls the whole row with acquire loads until every entry is non-zero.  When
-// a CTA has seen all of round t, every CTA has finished reading round t-1, so
-// it clears its own round-(t-1) entry, which it will not publish into again
-// before round t+2; the clear is ordered before its round t+1 release store,
-// so a reader of round t+2 can never see the stale value.
+// polls the whole row until every entry is non-zero.  Each lane issues the
+// loads of all its slots back to back (relaxed) so one poll costs one L2 round
+// trip; a fence after the last poll makes it an acquire.  When a CTA has seen
+// all of round t, every CTA has finished reading round t-1, so it clears its
+// own round-(t-1) entry, which it will not publish into again before round
+// t+2; the clear is ordered before its round t+1 release store, so a reader of
+// round t+2 can never see the stale value.
 //
 // A CTA without candidates publishes kKeyValid alone, which never beats a
-// real key of a valid point.  Returns 0 (and sets err) if a slot stays empty
-// for kSpinLimit polls.
+// real key of a valid point.  Returns 0 (and sets err) if the row is still
+// incomplete after kSpinLimit polls.
 __device__ __forceinline__ uint64_t exchange_max(uint64_t* slots, int G, uint32_t round,
                                                  uint64_t my_key, int* err) {
+    constexpr int kPer = kMaxGrid / 32;
     const int lane = threadIdx.x & 31;
     uint64_t* row = slots + (uint64_t)(round % 3u) * G;
     if (lane == 0) st_release_gpu(row + blockIdx.x, my_key | kKeyValid);
-    uint64_t best = 0;
-    bool ok = true;
-    for (int j = lane; j < G; j += 32) {
-        uint64_t v = 0;
-        long long spins = 0;
-        while ((v = ld_acquire_gpu(row + j)) == 0ull) {
-            if (++spins > kSpinLimit) {
-                ok = false;
-                break;
-            }
+    uint64_t v[kPer];
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) v[i] = 0;
+    long long spins = 0;
+    for (;;) {
+        bool mine = true;
+#pragma unroll
+        for (int i = 0; i < kPer; ++i) {
+            const int j = lane + 32 * i;
+            if (j < G && v[i] == 0) v[i] = ld_relaxed_gpu(row + j);
         }
-        best = v > best ? v : best;
+#pragma unroll
+        for (int i = 0; i < kPer; ++i) {
+            const int j = lane + 32 * i;
+            if (j < G && v[i] == 0) mine = false;
+        }
+        if (__all_sync(kFull, mine)) break;
+        if (++spins > kSpinLimit) {
+            if (lane == 0) atomicOr(err, kErrExchangeTimeout);
+            return 0;
+        }
     }
-    if (__any_sync(kFull, !ok)) {
-        if (lane == 0) atomicOr(err, kErrExchangeTimeout);
-        return 0;
-    }
+    fence_acq_rel_gpu();
+    uint64_t best = 0;
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) best = v[i] > best ? v[i] : best;
     best = warp_max_key(best);
     if (lane == 0) st_relaxed_gpu(slots + (uint64_t)((round + 2u) % 3u) * G + blockIdx.x, 0ull);
     return best;

@@ -77,8 +77,11 @@ int run_vanilla_fma(const VanillaCall& c);
 
 // The pruned engine (engine.cuh): kd-line QuickFPS and vanilla FPS.
 struct EngineCall;
+struct BatchCall;
 int run_engine_nofma(int dim, const EngineCall& c);
 int run_engine_fma(int dim, const EngineCall& c);
+int run_batch_nofma(int dim, const BatchCall& c);
+int run_batch_fma(int dim, const BatchCall& c);
 
 // measurement counters (fpsgpu_stats_*)
 void stats_count_launch(uint64_t n = 1);

@@ -133,6 +133,43 @@ Indices bucket_fps_kdline_sampling(FloatRows points, size_t n_samples, size_t he
     return out;
 }
 
+// Batched QuickFPS: clouds stored back to back in `points` (rows
+// [offsets[c], offsets[c+1]) form cloud c).  Returns one uint64 array with the
+// clouds' local indices back to back (cloud c at sum(n_samples[:c])).
+Indices bucket_fps_kdline_sampling_batch(FloatRows points, Indices offsets, Indices n_samples,
+                                         Indices heights, Indices starts) {
+    if (points.ndim() != 2) throw py::value_error("points must be a 2D float32 array");
+    const ssize_t C = n_samples.size();
+    if (offsets.size() != C + 1 || heights.size() != C || starts.size() != C)
+        throw py::value_error("offsets must have n_clouds + 1 entries; n_samples, heights and "
+                              "starts n_clouds");
+    const size_t* off = offsets.data();
+    if (C > 0 && (off[0] != 0 || off[C] != (size_t)points.shape(0)))
+        throw py::value_error("offsets must start at 0 and end at the number of points");
+    size_t total = 0;
+    for (ssize_t c = 0; c < C; ++c) {
+        const size_t nc = off[c + 1] - off[c];
+        const size_t k = n_samples.data()[c];
+        if (off[c + 1] < off[c] || nc == 0) throw py::value_error("empty cloud in the batch");
+        if (starts.data()[c] >= nc) throw py::value_error("start_idx out of range");
+        if (k == 0 || k > nc) throw py::value_error("n_samples must be in [1, num_points]");
+        if (heights.data()[c] == 0) throw py::value_error("height must be >= 1");
+        total += k;
+    }
+    Indices out(total);
+    if (C == 0) return out;
+    int rc;
+    const float* data = points.data();
+    size_t* out_ptr = static_cast<size_t*>(out.mutable_data());
+    {
+        py::gil_scoped_release nogil;
+        rc = fpsgpu_kdline_batch(data, off, (size_t)C, (size_t)points.shape(1), n_samples.data(),
+                                 starts.data(), heights.data(), out_ptr);
+    }
+    if (rc != 0) raise_gpu_failure("fpsgpu_kdline_batch", rc);
+    return out;
+}
+
 [[noreturn]] void not_in_gpu_build(const char* name) {
     PyErr_SetString(PyExc_NotImplementedError,
                     (std::string(name) +
@@ -219,6 +256,8 @@ PYBIND11_MODULE(_fpsample, m) {
     m.def("_bucket_fps_kdtree_sampling",
           [](py::args, py::kwargs) { not_in_gpu_build("_bucket_fps_kdtree_sampling"); });
 
+    m.def("_bucket_fps_kdline_sampling_batch", &bucket_fps_kdline_sampling_batch,
+          "many clouds in one GPU call: (points, offsets, n_samples, heights, starts) -> indices");
     m.def("_kdline_build", &kdline_build,
           "kd-line tree build alone: (perm uint64[N], bucket_starts uint64[B])");
     m.def("_get_fp_mode", &get_fp_mode, "current floating-point mode: 'nofma' or 'fma'");

@@ -83,6 +83,27 @@ int fpsgpu_fps_device(const float *d_points, size_t n_points, size_t dim,
                       uint64_t *d_out, float *d_trace, void *stream);
 
 /*
+ * Many clouds in one call: the batched form of bucket_fps_kdline.  Cloud c is
+ * rows [offsets[c], offsets[c+1]) of raw_data (offsets[0] == 0, n_clouds + 1
+ * entries); n_samples[c], start_idx[c] and height[c] mean what they mean in
+ * bucket_fps_kdline for that cloud alone, and the result is identical to
+ * calling it once per cloud.  Cloud c's indices (local to the cloud) are
+ * written at sampled_point_indices[n_samples[0] + ... + n_samples[c-1]].
+ * The reference has no batched entry point; its per-cloud equivalent is
+ * src/wrapper.hpp:118-132 called in a loop.  Host buffers; synchronous.
+ */
+int fpsgpu_kdline_batch(const float *raw_data, const size_t *offsets, size_t n_clouds,
+                        size_t dim, const size_t *n_samples, const size_t *start_idx,
+                        const size_t *height, size_t *sampled_point_indices);
+
+/* Device-buffer form of fpsgpu_kdline_batch: d_points and d_out are device
+   pointers, the per-cloud arrays are HOST arrays; stream as above. */
+int fpsgpu_kdline_batch_device(const float *d_points, const size_t *h_offsets,
+                               size_t n_clouds, size_t dim, const size_t *h_n_samples,
+                               const size_t *h_start_idx, const size_t *h_height,
+                               uint64_t *d_out, void *stream);
+
+/*
  * The kd-line tree build alone (KDTreeBase.h:84-207 of the reference), for
  * inspection and tests: h_perm (n_points, HOST) receives the original index of
  * the point at every position of the permuted order, h_bucket_start (HOST,

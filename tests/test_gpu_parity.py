@@ -175,3 +175,61 @@ def test_gmm_1m_vanilla_prefix():
     t = tr.cpu().numpy()
     assert np.all(np.diff(t[1:]) <= 0)
     assert len(np.unique(out)) == 16384
+
+
+def _batch_clouds(seed, count, lo, hi, d=3):
+    rng = np.random.default_rng(seed)
+    clouds, ks, hs, ss = [], [], [], []
+    for i in range(count):
+        n = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        kind = i % 3
+        if kind == 0:
+            p = rng.random((n, d)) * rng.uniform(0.1, 10, d)
+        elif kind == 1:
+            p = rng.integers(0, 6, (n, d))  # ties
+        else:
+            p = rng.standard_normal((n, d)) * 50
+        clouds.append(p.astype(np.float32))
+        ks.append(int(rng.integers(1, n + 1)))
+        hs.append(int(rng.integers(1, max(2, int(np.log2(n))) + 1)))
+        ss.append(int(rng.integers(0, n)))
+    return clouds, ks, hs, ss
+
+
+@pytest.mark.parametrize("seed,d", [(0, 3), (1, 1), (2, 5), (3, 8)])
+def test_batch_equals_oracle_per_cloud(seed, d, mode):
+    clouds, ks, hs, ss = _batch_clouds(seed, 24, 2, 20000, d)
+    got = fps.bucket_fps_kdline_sampling_batch(clouds, ks, hs, ss)
+    for p, k, h, s, g in zip(clouds, ks, hs, ss, got):
+        np.testing.assert_array_equal(g, ORACLE.kdline(p, k, h, s, mode))
+
+
+def test_batch_with_clouds_too_big_for_shared_memory(mode):
+    # one cloud with more piece records than fit in shared memory takes the
+    # multi-CTA path inside the same batched call
+    clouds, ks, hs, ss = _batch_clouds(7, 6, 500, 5000)
+    big = W.gmm_cloud(400_000, seed=8)
+    clouds.insert(2, big)
+    ks.insert(2, 3000)
+    hs.insert(2, 7)
+    ss.insert(2, 11)
+    got = capi.kdline_batch(clouds, ks, hs, ss)
+    for p, k, h, s, g in zip(clouds, ks, hs, ss, got):
+        np.testing.assert_array_equal(g, ORACLE.kdline(p, k, h, s, mode))
+
+
+def test_batch_identical_to_one_call_per_cloud():
+    clouds, ks, hs, ss = _batch_clouds(11, 40, 1000, 60000)
+    got = fps.bucket_fps_kdline_sampling_batch(clouds, ks, hs, ss)
+    for p, k, h, s, g in zip(clouds, ks, hs, ss, got):
+        np.testing.assert_array_equal(g, fps.bucket_fps_kdline_sampling(p, k, h, s))
+
+
+def test_batched_workload_sample_vs_oracle():
+    """The bench's 256-cloud workload: every 16th cloud checked against the oracle."""
+    clouds = W.batched_clouds(seed=W.SEEDS["batched-256"])
+    hs = [5 if p.shape[0] < 8192 else 7 for p, _ in clouds]
+    got = fps.bucket_fps_kdline_sampling_batch([p for p, _ in clouds], [k for _, k in clouds], hs, 0)
+    for i in range(0, len(clouds), 16):
+        p, k = clouds[i]
+        np.testing.assert_array_equal(got[i], ORACLE.kdline(p, k, hs[i], 0))
