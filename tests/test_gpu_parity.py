@@ -191,7 +191,7 @@ def _batch_clouds(seed, count, lo, hi, d=3):
             p = rng.standard_normal((n, d)) * 50
         clouds.append(p.astype(np.float32))
         ks.append(int(rng.integers(1, n + 1)))
-        hs.append(int(rng.integers(1, max(2, int(np.log2(n))) + 1)))
+        hs.append(int(rng.integers(1, max(1, int(np.log2(n))) + 1)))  # 2**h <= n
         ss.append(int(rng.integers(0, n)))
     return clouds, ks, hs, ss
 
