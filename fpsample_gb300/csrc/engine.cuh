@@ -624,16 +624,91 @@ __global__ void __launch_bounds__(kSampleThreads, 1) fps_sample(SampleArgs a) {
     }
 }
 
+// Recomputes one dirty piece [ps, pe) against reference point r: running
+// distances lowered with the reference's strict "<" rule (or initialised to
+// min(init, d) on the first pass), the piece's new max key and the coordinates
+// of its max point (broadcast to the whole warp).  xb/disb/tagb may point to
+// shared or global memory; xs is the coordinate stride.  Pieces of at most
+// kPiece points take an unrolled path that issues every load of the piece
+// before the first use, so a piece in global memory costs one round trip.
+template <int D, bool FMA, bool KD>
+__device__ __forceinline__ uint64_t recompute_piece(const float* xb, uint64_t xs, float* disb,
+                                                    const uint32_t* tagb, uint32_t ps, uint32_t pe,
+                                                    const float* r, bool first, float* c_out) {
+    const int lane = threadIdx.x & 31;
+    const float init = KD ? FLT_MAX : INFINITY;
+    uint64_t pk = 0;
+    float pc[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) pc[d] = 0.0f;
+    if (pe - ps <= kPiece) {
+        constexpr int PPL = kPiece / 32;
+        float x[PPL][D], dv[PPL];
+        uint32_t tg[PPL];
+#pragma unroll
+        for (int j = 0; j < PPL; ++j) {
+            const uint32_t p = ps + lane + 32 * j;
+            if (p < pe) {
+#pragma unroll
+                for (int d = 0; d < D; ++d) x[j][d] = xb[(uint64_t)d * xs + p];
+                dv[j] = first ? init : disb[p];
+                tg[j] = tagb[p];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < PPL; ++j) {
+            const uint32_t p = ps + lane + 32 * j;
+            if (p < pe) {
+                const float dd = sqdist<D, FMA>(x[j], r);
+                float v = dv[j];
+                if (dd < v) v = dd;
+                if (first || dd < dv[j]) disb[p] = v;
+                const uint64_t kk = make_key<KD>(v, tg[j]);
+                if (kk > pk) {
+                    pk = kk;
+#pragma unroll
+                    for (int d = 0; d < D; ++d) pc[d] = x[j][d];
+                }
+            }
+        }
+    } else {
+        for (uint32_t p = ps + lane; p < pe; p += 32) {
+            float x[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) x[d] = xb[(uint64_t)d * xs + p];
+            const float old = first ? init : disb[p];
+            const float dd = sqdist<D, FMA>(x, r);
+            float v = old;
+            if (dd < v) v = dd;
+            if (first || dd < old) disb[p] = v;
+            const uint64_t kk = make_key<KD>(v, tagb[p]);
+            if (kk > pk) {
+                pk = kk;
+#pragma unroll
+                for (int d = 0; d < D; ++d) pc[d] = x[d];
+            }
+        }
+    }
+    const uint64_t wk = warp_max_key(pk);
+    const int owner = __ffs(__ballot_sync(kFull, pk == wk)) - 1;
+#pragma unroll
+    for (int d = 0; d < D; ++d) c_out[d] = __shfl_sync(kFull, pc[d], owner);
+    return wk;
+}
+
 // ---- batched sampling: one CTA per cloud -------------------------------------
 //
 // A persistent grid pulls clouds from a queue (largest first).  The CTA keeps
-// its cloud's piece records in shared memory: max key, bounding box and the
-// coordinates of the max point.  One iteration is: every warp tests its pieces
-// against the reference point, recomputes the dirty ones from global memory,
-// and offers its best (key, piece); warp 0 picks the winner and reads the next
-// reference point from the winning piece's record.  Two __syncthreads per
-// sample, no cross-CTA communication, no global load for the winner.
-constexpr int kBatchThreads = 256;
+// its cloud's piece records in shared memory: max key, bounding box, start and
+// the coordinates of the max point; clouds of at most `mcap` points also keep
+// their points (coordinates, running distance, tag) there.  One iteration is:
+// every warp tests its pieces against the reference point, recomputes the
+// dirty ones, and offers its best (key, piece); warp 0 picks the winner and
+// reads the next reference point from the winning piece's record.  Two
+// __syncthreads per sample, no cross-CTA communication, no global load for the
+// winner.
+// 1024 threads per cloud (fewer for D > 4, where 64 registers would spill)
+constexpr int batch_threads(int D) { return D <= 4 ? 1024 : 512; }
 
 struct BatchArgs {
     const float* X;             // SoA [D][n], storage order (all clouds)
@@ -656,23 +731,31 @@ struct BatchArgs {
     unsigned int* queue;
     unsigned long long* counters;
     uint32_t cap;               // piece records that fit in shared memory
+    uint32_t mcap;              // points that fit in shared memory
 };
 
+inline size_t batch_smem_bytes(int D, uint32_t cap, uint32_t mcap) {
+    return (size_t)cap * (8 + 12 * D) + (size_t)(cap + 1) * 4 + (size_t)mcap * (4 * D + 8) + 16;
+}
+
 template <int D, bool FMA, bool KD>
-__global__ void __launch_bounds__(kBatchThreads) batch_sample(BatchArgs a) {
+__global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     __shared__ uint64_t s_wkey[32];
     __shared__ uint32_t s_wq[32];
     __shared__ float s_ref[kMaxDim];
     __shared__ uint32_t s_item;
-    const uint32_t cap = a.cap;
+    const uint32_t cap = a.cap, mcap = a.mcap;
     uint64_t* s_key = reinterpret_cast<uint64_t*>(s_dyn);
     float* s_lo = reinterpret_cast<float*>(s_key + cap);  // [D][cap]
     float* s_hi = s_lo + (size_t)D * cap;
     float* s_mc = s_hi + (size_t)D * cap;                 // coordinates of each piece's max
+    float* s_x = s_mc + (size_t)D * cap;                  // [D][mcap]
+    float* s_dis = s_x + (size_t)D * mcap;                // [mcap]
+    uint32_t* s_tag = reinterpret_cast<uint32_t*>(s_dis + mcap);  // [mcap]
+    uint32_t* s_ps = s_tag + mcap;                        // [cap + 1] local piece starts
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const uint64_t n = a.n;
-    const float init = KD ? FLT_MAX : INFINITY;
     unsigned long long tested = 0, touched = 0;
 
     for (;;) {
@@ -685,14 +768,30 @@ __global__ void __launch_bounds__(kBatchThreads) batch_sample(BatchArgs a) {
         const uint32_t np = a.cloud_piece[c + 1] - P0;
         const uint64_t K = a.cloud_k[c];
         const uint64_t coff = a.cloud_off[c];
+        const uint32_t nc = (uint32_t)(a.cloud_off[c + 1] - coff);
         const uint64_t ooff = a.out_off[c];
-        for (uint32_t i = tid; i < np; i += blockDim.x) {
+        const bool resident = nc <= mcap;
+        for (uint32_t i = tid; i <= np; i += blockDim.x) {
+            s_ps[i] = a.pstart[P0 + i] - (uint32_t)coff;
+            if (i < np) {
 #pragma unroll
-            for (int d = 0; d < D; ++d) {
-                s_lo[(size_t)d * cap + i] = a.plo[(uint64_t)(P0 + i) * D + d];
-                s_hi[(size_t)d * cap + i] = a.phi[(uint64_t)(P0 + i) * D + d];
+                for (int d = 0; d < D; ++d) {
+                    s_lo[(size_t)d * cap + i] = a.plo[(uint64_t)(P0 + i) * D + d];
+                    s_hi[(size_t)d * cap + i] = a.phi[(uint64_t)(P0 + i) * D + d];
+                }
             }
         }
+        if (resident) {
+            for (uint32_t i = tid; i < nc; i += blockDim.x) {
+#pragma unroll
+                for (int d = 0; d < D; ++d) s_x[(size_t)d * mcap + i] = a.X[(uint64_t)d * n + coff + i];
+                s_tag[i] = a.tag[coff + i];
+            }
+        }
+        const float* xb = resident ? s_x : a.X + coff;
+        const uint64_t xs = resident ? mcap : n;
+        float* disb = resident ? s_dis : a.dis + coff;
+        const uint32_t* tagb = resident ? s_tag : a.tag + coff;
         const uint32_t tag0 = (uint32_t)a.cloud_tag0[c];
         if (tid < D) s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
         if (tid == 0 && K > 0) a.out[ooff] = (KD ? a.idmap[tag0] : tag0) - coff;
@@ -727,34 +826,11 @@ __global__ void __launch_bounds__(kBatchThreads) batch_sample(BatchArgs a) {
                     const int l = __ffs(m) - 1;
                     m &= m - 1;
                     const uint32_t qq = qb + l;
-                    const uint32_t ps = __ldg(a.pstart + P0 + qq), pe = __ldg(a.pstart + P0 + qq + 1);
+                    const uint32_t ps = s_ps[qq], pe = s_ps[qq + 1];
                     touched += pe - ps;
-                    uint64_t pk = 0;
                     float pc[D];
-#pragma unroll
-                    for (int d = 0; d < D; ++d) pc[d] = 0.0f;
-                    for (uint32_t p = ps + lane; p < pe; p += 32) {
-                        float x[D];
-#pragma unroll
-                        for (int d = 0; d < D; ++d) x[d] = __ldg(a.X + (uint64_t)d * n + p);
-                        float dv = t == 0 ? init : a.dis[p];
-                        const float dd = sqdist<D, FMA>(x, r);
-                        if (dd < dv) {
-                            dv = dd;
-                            if (t > 0) a.dis[p] = dv;
-                        }
-                        if (t == 0) a.dis[p] = dv;
-                        const uint64_t kk = make_key<KD>(dv, __ldg(a.tag + p));
-                        if (kk > pk) {
-                            pk = kk;
-#pragma unroll
-                            for (int d = 0; d < D; ++d) pc[d] = x[d];
-                        }
-                    }
-                    const uint64_t wk = warp_max_key(pk);
-                    const int owner = __ffs(__ballot_sync(kFull, pk == wk)) - 1;
-#pragma unroll
-                    for (int d = 0; d < D; ++d) pc[d] = __shfl_sync(kFull, pc[d], owner);
+                    const uint64_t wk =
+                        recompute_piece<D, FMA, KD>(xb, xs, disb, tagb, ps, pe, r, t == 0, pc);
                     if (lane == l) {
                         key = wk;
                         s_key[qq] = wk;
@@ -979,6 +1055,315 @@ inline int check_device_error(const int* d_err, cudaStream_t stream) {
     return FPSGPU_OK;
 }
 
+// ---- grid sampling with shared-memory residency ------------------------------
+//
+// For one large cloud: every CTA of a cooperative grid owns a contiguous run of
+// pieces and keeps their points (coordinates, running distance, tag) and piece
+// records (max key, box, coordinates of the max) in shared memory for the
+// whole run.  One iteration = shared-memory work, one __syncthreads, and one
+// exchange_max_coords round trip that also delivers the next reference point.
+constexpr int kSmemThreads = 512;
+
+struct GridSmemArgs {
+    const float* X;
+    const uint32_t* tag;
+    uint64_t n;
+    const uint32_t* pstart;     // global piece starts
+    const float* plo;
+    const float* phi;
+    const uint32_t* cta_piece;  // [G + 1] global piece index where each CTA starts
+    uint32_t maxq, maxm;        // shared-memory layout: pieces / points per CTA
+    const float* Xref;
+    const uint32_t* idmap;
+    uint64_t k;
+    const uint64_t* forced;
+    uint32_t n_forced;
+    uint64_t id_offset;
+    uint64_t* out;
+    float* trace;
+    uint64_t* slots;
+    int* err;
+    unsigned long long* counters;
+};
+
+inline size_t grid_smem_bytes(int D, uint32_t maxq, uint32_t maxm) {
+    return (size_t)maxq * (8 + 12 * D) + (size_t)maxm * (4 * D + 8) + (size_t)(maxq + 1) * 4 + 16;
+}
+
+template <int D, bool FMA, bool KD>
+__global__ void __launch_bounds__(kSmemThreads, 1) grid_sample_smem(GridSmemArgs a) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    const uint32_t MQ = a.maxq, MM = a.maxm;
+    uint64_t* s_key = reinterpret_cast<uint64_t*>(s_dyn);
+    float* s_lo = reinterpret_cast<float*>(s_key + MQ);
+    float* s_hi = s_lo + (size_t)D * MQ;
+    float* s_mc = s_hi + (size_t)D * MQ;
+    float* s_x = s_mc + (size_t)D * MQ;
+    float* s_dis = s_x + (size_t)D * MM;
+    uint32_t* s_tag = reinterpret_cast<uint32_t*>(s_dis + MM);
+    uint32_t* s_ps = s_tag + MM;
+    __shared__ uint64_t s_wkey[32];
+    __shared__ uint32_t s_wq[32];
+    __shared__ float s_ref[kMaxDim];
+    __shared__ int s_abort;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const int G = gridDim.x;
+    const uint64_t n = a.n;
+    const uint32_t P0 = a.cta_piece[blockIdx.x];
+    const uint32_t nq = a.cta_piece[blockIdx.x + 1] - P0;
+    const uint32_t S0 = a.pstart[P0];
+    const uint32_t m = a.pstart[P0 + nq] - S0;
+    const float init = KD ? FLT_MAX : INFINITY;
+
+    for (uint32_t i = tid; i < m; i += blockDim.x) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) s_x[(size_t)d * MM + i] = a.X[(uint64_t)d * n + S0 + i];
+        s_tag[i] = a.tag[S0 + i];
+    }
+    for (uint32_t q = tid; q <= nq; q += blockDim.x) {
+        s_ps[q] = a.pstart[P0 + q] - S0;
+        if (q < nq) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                s_lo[(size_t)d * MQ + q] = a.plo[(uint64_t)(P0 + q) * D + d];
+                s_hi[(size_t)d * MQ + q] = a.phi[(uint64_t)(P0 + q) * D + d];
+            }
+        }
+    }
+    const uint32_t tag0 = (uint32_t)a.forced[0];
+    if (tid < D) s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
+    if (tid == 0) s_abort = 0;
+    if (blockIdx.x == 0 && tid == 0 && a.k > 0) {
+        a.out[0] = (KD ? a.idmap[tag0] : tag0) - a.id_offset;
+        if (a.trace) a.trace[0] = init;
+    }
+    __syncthreads();
+    const uint32_t pw = (nq + nwarps - 1) / nwarps;
+    const uint32_t q0 = warp * pw < nq ? warp * pw : nq;
+    const uint32_t q1 = q0 + pw < nq ? q0 + pw : nq;
+
+    uint32_t xround = 0;
+    unsigned long long tested = 0, touched = 0;
+    for (uint64_t t = 0; t + 1 < a.k; ++t) {
+        float r[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) r[d] = s_ref[d];
+        uint64_t best = 0;
+        uint32_t bestq = 0;
+        if (t > 0) tested += q1 - q0;
+        for (uint32_t qb = q0; qb < q1; qb += 32) {
+            const uint32_t q = qb + lane;
+            const bool have = q < q1;
+            uint64_t key = have && t > 0 ? s_key[q] : 0ull;
+            bool dirty = have;
+            if (have && t > 0) {
+                float lo[D], hi[D];
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    lo[d] = s_lo[(size_t)d * MQ + q];
+                    hi[d] = s_hi[(size_t)d * MQ + q];
+                }
+                dirty = box_bound<D, FMA>(lo, hi, r) < key_dist(key);
+            }
+            uint32_t msk = __ballot_sync(kFull, dirty);
+            while (msk) {
+                const int l = __ffs(msk) - 1;
+                msk &= msk - 1;
+                const uint32_t qq = qb + l;
+                const uint32_t ps = s_ps[qq], pe = s_ps[qq + 1];
+                touched += pe - ps;
+                uint64_t pk = 0;
+                float pc[D];
+#pragma unroll
+                for (int d = 0; d < D; ++d) pc[d] = 0.0f;
+                for (uint32_t i = ps + lane; i < pe; i += 32) {
+                    float x[D];
+#pragma unroll
+                    for (int d = 0; d < D; ++d) x[d] = s_x[(size_t)d * MM + i];
+                    float dv = t == 0 ? init : s_dis[i];
+                    const float dd = sqdist<D, FMA>(x, r);
+                    if (dd < dv) dv = dd;
+                    s_dis[i] = dv;
+                    const uint64_t kk = make_key<KD>(dv, s_tag[i]);
+                    if (kk > pk) {
+                        pk = kk;
+#pragma unroll
+                        for (int d = 0; d < D; ++d) pc[d] = x[d];
+                    }
+                }
+                const uint64_t wk = warp_max_key(pk);
+                const int owner = __ffs(__ballot_sync(kFull, pk == wk)) - 1;
+#pragma unroll
+                for (int d = 0; d < D; ++d) pc[d] = __shfl_sync(kFull, pc[d], owner);
+                if (lane == l) {
+                    key = wk;
+                    s_key[qq] = wk;
+#pragma unroll
+                    for (int d = 0; d < D; ++d) s_mc[(size_t)d * MQ + qq] = pc[d];
+                }
+            }
+            if (have && key > best) {
+                best = key;
+                bestq = q;
+            }
+        }
+        const uint64_t wb = warp_max_key(best);
+        const int wl = __ffs(__ballot_sync(kFull, best == wb)) - 1;
+        bestq = __shfl_sync(kFull, bestq, wl);
+        const bool forced = t + 1 < a.n_forced;
+        if (lane == 0) {
+            s_wkey[warp] = wb;
+            s_wq[warp] = bestq;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            uint64_t g = 0;
+            uint32_t tg = 0;
+            bool ok = true;
+            float wc[D];
+            if (forced) {
+                tg = (uint32_t)a.forced[t + 1];
+#pragma unroll
+                for (int d = 0; d < D; ++d) wc[d] = a.Xref[(uint64_t)d * n + tg];
+            } else {
+                const uint64_t kw = lane < nwarps ? s_wkey[lane] : 0ull;
+                g = warp_max_key(kw);
+                const int w = __ffs(__ballot_sync(kFull, lane < nwarps && kw == g)) - 1;
+                const uint32_t qwin = s_wq[w];
+                float mc[D];
+#pragma unroll
+                for (int d = 0; d < D; ++d) mc[d] = nq > 0 ? s_mc[(size_t)d * MQ + qwin] : 0.0f;
+                if (G > 1) {
+                    g = exchange_max_coords<D>(a.slots, G, xround++, g, mc, wc, a.err);
+                } else {
+#pragma unroll
+                    for (int d = 0; d < D; ++d) wc[d] = mc[d];
+                }
+                ok = g != 0;
+                tg = key_pos<KD>(g);
+                if (ok && tg >= n) {
+                    ok = false;
+                    if (lane == 0) atomicOr(a.err, kErrBadIndex);
+                }
+            }
+            if (!ok) {
+                if (lane == 0) s_abort = 1;
+            } else {
+#pragma unroll
+                for (int d = 0; d < D; ++d)
+                    if (lane == d) s_ref[d] = wc[d];  // static indices keep wc in registers
+                if (blockIdx.x == 0 && lane == 0) {
+                    a.out[t + 1] = (KD ? a.idmap[tg] : tg) - a.id_offset;
+                    if (a.trace) a.trace[t + 1] = forced ? INFINITY : key_dist(g);
+                }
+            }
+        }
+        __syncthreads();
+        if (s_abort) break;
+    }
+    if (a.counters && lane == 0) {
+        atomicAdd(a.counters, tested);
+        atomicAdd(a.counters + 1, touched);
+    }
+}
+
+constexpr int kNoFit = -1;
+
+// The shared-memory-resident grid sampler, if the range fits on chip;
+// returns kNoFit (nothing launched) otherwise.
+template <int D, bool FMA>
+int sample_grid_smem(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint32_t np,
+                     uint64_t k, const uint64_t* h_forced, uint32_t n_forced, uint64_t id_offset,
+                     uint64_t* d_out, float* d_trace, cudaStream_t stream, int sms, Scratch& sc) {
+    int rc;
+    if (np == ~0u) {
+        uint32_t h_np = 0;
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(&h_np, bt.d_np, 4, cudaMemcpyDeviceToHost, stream));
+        FPSGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+        np = h_np;
+    }
+    if (np == 0) return kNoFit;
+    std::vector<uint32_t> ps(np + 1);
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(ps.data(), bt.pstart + piece0, (np + 1) * 4,
+                                    cudaMemcpyDeviceToHost, stream));
+    FPSGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+    const uint64_t pts = ps[np] - ps[0];
+    int dev = 0, smem_max = 0;
+    FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
+    FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const size_t budget = (size_t)smem_max - 1024;  // static shared memory
+    uint64_t G = std::min<uint64_t>({(uint64_t)sms, (uint64_t)kMaxGridCoords,
+                                     std::max<uint64_t>(1, pts / 2048)});
+    // cut the piece range at the pieces nearest to equal point shares
+    std::vector<uint32_t> cut(G + 1);
+    cut[0] = 0;
+    cut[G] = np;
+    for (uint64_t c = 1; c < G; ++c) {
+        const uint64_t target = ps[0] + pts * c / G;
+        cut[c] = (uint32_t)(std::lower_bound(ps.begin(), ps.end() - 1, (uint32_t)target) - ps.begin());
+        cut[c] = std::max(cut[c], cut[c - 1]);
+    }
+    uint32_t maxq = 1, maxm = 1;
+    for (uint64_t c = 0; c < G; ++c) {
+        maxq = std::max(maxq, cut[c + 1] - cut[c]);
+        maxm = std::max(maxm, ps[cut[c + 1]] - ps[cut[c]]);
+    }
+    const size_t smem = grid_smem_bytes(D, maxq, maxm);
+    if (smem > budget) return kNoFit;
+    for (auto& x : cut) x += piece0;
+
+    uint32_t* d_cut;
+    uint64_t* slots;
+    uint64_t* d_forced;
+    unsigned long long* cnt;
+    const uint64_t nslots = 3 * G * (1 + D);
+    if ((rc = sc.alloc(&d_cut, G + 1))) return rc;
+    if ((rc = sc.alloc(&slots, nslots))) return rc;
+    if ((rc = sc.alloc(&d_forced, n_forced))) return rc;
+    if ((rc = sc.alloc(&cnt, 2))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_cut, cut.data(), (G + 1) * 4, cudaMemcpyHostToDevice, stream));
+    FPSGPU_CUDA_TRY(cudaMemsetAsync(slots, 0, nslots * sizeof(uint64_t), stream));
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_forced, h_forced, n_forced * sizeof(uint64_t),
+                                    cudaMemcpyHostToDevice, stream));
+    FPSGPU_CUDA_TRY(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), stream));
+    GridSmemArgs a{};
+    a.X = bt.X;
+    a.tag = bt.tag;
+    a.n = n;
+    a.pstart = bt.pstart;
+    a.plo = bt.plo;
+    a.phi = bt.phi;
+    a.cta_piece = d_cut;
+    a.maxq = maxq;
+    a.maxm = maxm;
+    a.Xref = bt.Xref;
+    a.idmap = bt.idsnap;
+    a.k = k;
+    a.forced = d_forced;
+    a.n_forced = n_forced;
+    a.id_offset = id_offset;
+    a.out = d_out;
+    a.trace = d_trace;
+    a.slots = slots;
+    a.err = bt.err;
+    a.counters = cnt;
+    const void* kern = kd ? (const void*)grid_sample_smem<D, FMA, true>
+                          : (const void*)grid_sample_smem<D, FMA, false>;
+    FPSGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    void* args[] = {&a};
+    SamplerTimer timer;
+    timer.begin(stream);
+    if ((rc = launch_persistent(kern, (int)G, kSmemThreads, args, smem, stream, G > 1))) return rc;
+    timer.end(stream);
+    unsigned long long h_cnt[2] = {0, 0};
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, stream));
+    if ((rc = check_device_error(bt.err, stream))) return rc;
+    const uint64_t cn[2] = {h_cnt[0], h_cnt[1]};
+    timer.finish(k, cn);
+    return FPSGPU_OK;
+}
+
 // Multi-CTA sampler over pieces [piece0, piece0 + np) (np == ~0u: the device
 // count of the whole build).
 template <int D, bool FMA>
@@ -986,7 +1371,9 @@ int sample_grid(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint32_t 
                 uint64_t points_in_range, uint64_t k, const uint64_t* h_forced, uint32_t n_forced,
                 uint64_t id_offset, uint64_t* d_out, float* d_trace, cudaStream_t stream, int sms,
                 Scratch& sc) {
-    int rc;
+    int rc = sample_grid_smem<D, FMA>(bt, n, kd, piece0, np, k, h_forced, n_forced, id_offset,
+                                      d_out, d_trace, stream, sms, sc);
+    if (rc != kNoFit) return rc;
     float* dis;
     uint64_t* pkey;
     const uint64_t nkeys = np == ~0u ? bt.np_cap : np;
@@ -1116,8 +1503,6 @@ struct BatchCall {
     int sms;
 };
 
-constexpr size_t kBatchSmemMax = 100 * 1024;
-
 template <int D, bool FMA>
 int run_batch(const BatchCall& bc) {
     Scratch sc(bc.stream);
@@ -1147,8 +1532,12 @@ int run_batch(const BatchCall& bc) {
                                     cudaMemcpyDeviceToHost, bc.stream));
     if ((rc = check_device_error(bt.err, bc.stream))) return rc;
 
-    const size_t rec = sizeof(uint64_t) + 3 * D * sizeof(float);
-    const uint32_t cap_max = (uint32_t)(kBatchSmemMax / rec);
+    int dev = 0, smem_optin = 0;
+    FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
+    FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const size_t avail = (size_t)smem_optin - 1024;  // static shared memory
+    const size_t rec = sizeof(uint64_t) + 3 * D * sizeof(float) + sizeof(uint32_t);
+    const uint32_t cap_max = (uint32_t)(avail / 2 / rec);
     std::vector<uint64_t> out_off(C), tag0(C);
     std::vector<uint32_t> small, big;
     uint64_t acc = 0;
@@ -1214,18 +1603,23 @@ int run_batch(const BatchCall& bc) {
         a.queue = d_queue;
         a.counters = cnt;
         a.cap = cap;
-        const size_t smem = (size_t)cap * rec;
+        // what the piece records leave of shared memory holds small clouds' points
+        uint64_t max_nc = 0;
+        for (uint32_t c : small) max_nc = std::max<uint64_t>(max_nc, bc.off[c + 1] - bc.off[c]);
+        const size_t left = avail - batch_smem_bytes(D, cap, 0);
+        a.mcap = (uint32_t)std::min<uint64_t>(left / (4 * D + 8), max_nc);
+        const size_t smem = batch_smem_bytes(D, cap, a.mcap);
         const void* kern = bc.kd ? (const void*)batch_sample<D, FMA, true>
                                  : (const void*)batch_sample<D, FMA, false>;
         FPSGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem));
         int per_sm = 0;
-        FPSGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBatchThreads, smem));
+        FPSGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, batch_threads(D), smem));
         const int G = (int)std::min<uint64_t>(small.size(), (uint64_t)std::max(1, per_sm) * bc.sms);
         void* args[] = {&a};
         SamplerTimer timer;
         timer.begin(bc.stream);
-        if ((rc = launch_persistent(kern, G, kBatchThreads, args, smem, bc.stream, false))) return rc;
+        if ((rc = launch_persistent(kern, G, batch_threads(D), args, smem, bc.stream, false))) return rc;
         timer.end(bc.stream);
         unsigned long long h_cnt[2] = {0, 0};
         FPSGPU_CUDA_TRY(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, bc.stream));

@@ -233,3 +233,13 @@ def test_batched_workload_sample_vs_oracle():
     for i in range(0, len(clouds), 16):
         p, k = clouds[i]
         np.testing.assert_array_equal(got[i], ORACLE.kdline(p, k, hs[i], 0))
+
+
+def test_cloud_beyond_shared_memory_uses_global_sampler(mode):
+    """1.2M points in 8 dimensions do not fit the grid's shared memory; the
+    global-memory sampler takes over and must give the same answer."""
+    rng = np.random.default_rng(21)
+    pts = rng.random((1_200_000, 8), dtype=np.float32)
+    np.testing.assert_array_equal(fps.bucket_fps_kdline_sampling(pts, 1500, 6, 5),
+                                  ORACLE.kdline(pts, 1500, 6, 5, mode))
+    np.testing.assert_array_equal(fps.fps_sampling(pts, 300, 5), ORACLE.fps(pts, 300, 5, mode))
