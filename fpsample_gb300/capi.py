@@ -26,6 +26,7 @@ SIGNATURES = {
     "fpsgpu_fps": (ctypes.c_int, [_f32p, _sz, _sz, _sz, _szp, _sz, _szp]),
     "fpsgpu_kdline_device": (ctypes.c_int, [_vp, _sz, _sz, _sz, _sz, _sz, _vp, _vp, _vp]),
     "fpsgpu_fps_device": (ctypes.c_int, [_vp, _sz, _sz, _sz, _szp, _sz, _vp, _vp, _vp]),
+    "fpsgpu_fps_device_noalloc": (ctypes.c_int, [_vp, _sz, _sz, _sz, _szp, _sz, _vp, _vp, _vp]),
     "fpsgpu_kdline_build": (ctypes.c_int, [_f32p, _sz, _sz, _sz, _u64p, _u64p, _szp]),
     "fpsgpu_kdline_batch": (ctypes.c_int, [_f32p, _szp, _sz, _sz, _szp, _szp, _szp, _szp]),
     "fpsgpu_kdline_batch_device": (ctypes.c_int, [_vp, _szp, _sz, _sz, _szp, _szp, _szp, _vp, _vp]),
@@ -219,3 +220,13 @@ def kdline_batch_device(points_ptr: int, offsets, dim: int, n_samples, heights, 
                                           ks.ctypes.data_as(_szp), ss.ctypes.data_as(_szp),
                                           hs.ctypes.data_as(_szp), out_ptr, stream or None)
     _check("fpsgpu_kdline_batch_device", rc)
+
+
+def fps_device_noalloc(points_ptr: int, n: int, dim: int, n_samples: int, starts, out_ptr: int,
+                       trace_ptr: int = 0, stream: int = 0) -> None:
+    """fpsgpu_fps_device_noalloc: vanilla FPS whose scratch is a fixed array in
+    the library (no GPU allocation; at most 65536 points, 512 starts)."""
+    st = np.atleast_1d(np.asarray(starts, dtype=np.uint64))
+    rc = lib().fpsgpu_fps_device_noalloc(points_ptr, n, dim, n_samples, st.ctypes.data_as(_szp),
+                                         st.size, out_ptr, trace_ptr or None, stream or None)
+    _check("fpsgpu_fps_device_noalloc", rc)

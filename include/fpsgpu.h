@@ -83,6 +83,22 @@ int fpsgpu_fps_device(const float *d_points, size_t n_points, size_t dim,
                       uint64_t *d_out, float *d_trace, void *stream);
 
 /*
+ * Vanilla FPS that allocates no GPU memory (no counterpart in the reference;
+ * same semantics and results as fpsgpu_fps_device).  For callers that cannot
+ * call cudaMalloc -- memory owned by another allocator or pool, a loop with a
+ * no-allocation rule, a device already fully reserved.  Its scratch is a fixed
+ * 4.4 KB __device__ array inside the library: at most 65536 points, 512 start
+ * indices, dim in [1, 8] (larger requests return FPSGPU_ERR_ARG).  All calls
+ * share that array, so calls whose GPU work overlaps (two streams, two host
+ * threads) race and must be serialised.  The first call on a device looks up
+ * the array's address; make it before any stream capture.  stream NULL means
+ * the legacy default stream.
+ */
+int fpsgpu_fps_device_noalloc(const float *d_points, size_t n_points, size_t dim,
+                              size_t n_samples, const size_t *h_start, size_t n_start,
+                              uint64_t *d_out, float *d_trace, void *stream);
+
+/*
  * Many clouds in one call: the batched form of bucket_fps_kdline.  Cloud c is
  * rows [offsets[c], offsets[c+1]) of raw_data (offsets[0] == 0, n_clouds + 1
  * entries); n_samples[c], start_idx[c] and height[c] mean what they mean in
