@@ -239,6 +239,12 @@ int compact_flags(const uint8_t* flag, uint64_t n, uint32_t* starts, uint32_t* d
     return FPSGPU_OK;
 }
 
+__global__ void map_tags(uint64_t* out, uint64_t k, const uint32_t* idmap, uint64_t id_offset) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < k;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = idmap[out[i]] - id_offset;
+}
+
 __global__ void cloud_piece_ranges(const uint32_t* pstart, const uint32_t* npieces,
                                    const uint64_t* cloud_off, uint32_t n_clouds, uint32_t* out) {
     const uint32_t np = *npieces;

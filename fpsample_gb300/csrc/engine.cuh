@@ -572,7 +572,7 @@ __global__ void __launch_bounds__(kSampleThreads, 1) fps_sample(SampleArgs a) {
     if (tid < D) s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
     if (tid == 0) s_abort = 0;
     if (blockIdx.x == 0 && tid == 0 && a.k > 0) {
-        a.out[0] = (KD ? a.idmap[tag0] : tag0) - a.id_offset;
+        a.out[0] = KD ? tag0 : tag0 - a.id_offset;
         if (a.trace) a.trace[0] = KD ? FLT_MAX : INFINITY;
     }
     __syncthreads();
@@ -597,7 +597,11 @@ __global__ void __launch_bounds__(kSampleThreads, 1) fps_sample(SampleArgs a) {
                 tg = (uint32_t)a.forced[t + 1];
             } else {
                 g = warp_max_key(lane < nwarps ? s_wkey[lane] : 0ull);
-                if (G > 1) g = exchange_max(a.slots, G, xround++, g, a.err);
+                if (G > 1) {
+                    float none[1];
+                    g = exchange_leader<0>(a.slots, a.slots + (uint64_t)G * leader_words<0>(), G,
+                                           xround++, g, none, none, a.err);
+                }
                 ok = g != 0;
                 tg = key_pos<KD>(g);
             }
@@ -610,7 +614,7 @@ __global__ void __launch_bounds__(kSampleThreads, 1) fps_sample(SampleArgs a) {
             } else {
                 if (lane < D) s_ref[lane] = a.Xref[(uint64_t)lane * n + tg];
                 if (blockIdx.x == 0 && lane == 0) {
-                    a.out[t + 1] = (KD ? a.idmap[tg] : tg) - a.id_offset;
+                    a.out[t + 1] = KD ? tg : tg - a.id_offset;
                     if (a.trace) a.trace[t + 1] = forced ? INFINITY : key_dist(g);
                 }
             }
@@ -794,11 +798,11 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
         const uint32_t* tagb = resident ? s_tag : a.tag + coff;
         const uint32_t tag0 = (uint32_t)a.cloud_tag0[c];
         if (tid < D) s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
-        if (tid == 0 && K > 0) a.out[ooff] = (KD ? a.idmap[tag0] : tag0) - coff;
+        // outputs hold tags while sampling (kd-line tags become original
+        // indices after the loop, off the per-sample critical path)
+        if (tid == 0 && K > 0) a.out[ooff] = KD ? tag0 : tag0 - coff;
         __syncthreads();
-        const uint32_t pw = (np + nwarps - 1) / nwarps;
-        const uint32_t q0 = warp * pw < np ? warp * pw : np;
-        const uint32_t q1 = q0 + pw < np ? q0 + pw : np;
+        const uint32_t stride = 32u * nwarps;  // piece q belongs to warp q % nwarps
 
         for (uint64_t t = 0; t + 1 < K; ++t) {
             float r[D];
@@ -806,10 +810,11 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
             for (int d = 0; d < D; ++d) r[d] = s_ref[d];
             uint64_t best = 0;
             uint32_t bestq = 0;
-            if (t > 0) tested += q1 - q0;
-            for (uint32_t qb = q0; qb < q1; qb += 32) {
-                const uint32_t q = qb + lane;
-                const bool have = q < q1;
+            for (uint32_t qb = 0; qb < np; qb += stride) {
+                const uint32_t q = qb + lane * nwarps + warp;
+                const bool have = q < np;
+                const uint32_t hb = __ballot_sync(kFull, have);
+                if (t > 0 && lane == 0) tested += __popc(hb);
                 uint64_t key = have && t > 0 ? s_key[q] : 0ull;
                 bool dirty = have;
                 if (have && t > 0) {
@@ -825,7 +830,7 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
                 while (m) {
                     const int l = __ffs(m) - 1;
                     m &= m - 1;
-                    const uint32_t qq = qb + l;
+                    const uint32_t qq = qb + l * nwarps + warp;
                     const uint32_t ps = s_ps[qq], pe = s_ps[qq + 1];
                     touched += pe - ps;
                     float pc[D];
@@ -859,10 +864,14 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
                 if (lane < D) s_ref[lane] = s_mc[(size_t)lane * cap + qwin];
                 if (lane == 0) {
                     const uint32_t tg = key_pos<KD>(g);
-                    a.out[ooff + t + 1] = (KD ? a.idmap[tg] : tg) - coff;
+                    a.out[ooff + t + 1] = KD ? tg : tg - coff;
                 }
             }
             __syncthreads();
+        }
+        if (KD) {
+            for (uint64_t i = tid; i < K; i += blockDim.x)
+                a.out[ooff + i] = a.idmap[a.out[ooff + i]] - coff;
         }
     }
     if (a.counters && lane == 0) {
@@ -1134,14 +1143,13 @@ __global__ void __launch_bounds__(kSmemThreads, 1) grid_sample_smem(GridSmemArgs
     const uint32_t tag0 = (uint32_t)a.forced[0];
     if (tid < D) s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
     if (tid == 0) s_abort = 0;
+    // outputs hold tags while sampling; kd-line tags are mapped afterwards
     if (blockIdx.x == 0 && tid == 0 && a.k > 0) {
-        a.out[0] = (KD ? a.idmap[tag0] : tag0) - a.id_offset;
+        a.out[0] = KD ? tag0 : tag0 - a.id_offset;
         if (a.trace) a.trace[0] = init;
     }
     __syncthreads();
-    const uint32_t pw = (nq + nwarps - 1) / nwarps;
-    const uint32_t q0 = warp * pw < nq ? warp * pw : nq;
-    const uint32_t q1 = q0 + pw < nq ? q0 + pw : nq;
+    const uint32_t stride = 32u * nwarps;  // piece q belongs to warp q % nwarps
 
     uint32_t xround = 0;
     unsigned long long tested = 0, touched = 0;
@@ -1151,10 +1159,11 @@ __global__ void __launch_bounds__(kSmemThreads, 1) grid_sample_smem(GridSmemArgs
         for (int d = 0; d < D; ++d) r[d] = s_ref[d];
         uint64_t best = 0;
         uint32_t bestq = 0;
-        if (t > 0) tested += q1 - q0;
-        for (uint32_t qb = q0; qb < q1; qb += 32) {
-            const uint32_t q = qb + lane;
-            const bool have = q < q1;
+        for (uint32_t qb = 0; qb < nq; qb += stride) {
+            const uint32_t q = qb + lane * nwarps + warp;
+            const bool have = q < nq;
+            const uint32_t hb = __ballot_sync(kFull, have);
+            if (t > 0 && lane == 0) tested += __popc(hb);
             uint64_t key = have && t > 0 ? s_key[q] : 0ull;
             bool dirty = have;
             if (have && t > 0) {
@@ -1170,7 +1179,7 @@ __global__ void __launch_bounds__(kSmemThreads, 1) grid_sample_smem(GridSmemArgs
             while (msk) {
                 const int l = __ffs(msk) - 1;
                 msk &= msk - 1;
-                const uint32_t qq = qb + l;
+                const uint32_t qq = qb + l * nwarps + warp;
                 const uint32_t ps = s_ps[qq], pe = s_ps[qq + 1];
                 touched += pe - ps;
                 uint64_t pk = 0;
@@ -1235,7 +1244,8 @@ __global__ void __launch_bounds__(kSmemThreads, 1) grid_sample_smem(GridSmemArgs
 #pragma unroll
                 for (int d = 0; d < D; ++d) mc[d] = nq > 0 ? s_mc[(size_t)d * MQ + qwin] : 0.0f;
                 if (G > 1) {
-                    g = exchange_max_coords<D>(a.slots, G, xround++, g, mc, wc, a.err);
+                    g = exchange_leader<D>(a.slots, a.slots + (uint64_t)G * leader_words<D>(), G,
+                                           xround++, g, mc, wc, a.err);
                 } else {
 #pragma unroll
                     for (int d = 0; d < D; ++d) wc[d] = mc[d];
@@ -1254,7 +1264,7 @@ __global__ void __launch_bounds__(kSmemThreads, 1) grid_sample_smem(GridSmemArgs
                 for (int d = 0; d < D; ++d)
                     if (lane == d) s_ref[d] = wc[d];  // static indices keep wc in registers
                 if (blockIdx.x == 0 && lane == 0) {
-                    a.out[t + 1] = (KD ? a.idmap[tg] : tg) - a.id_offset;
+                    a.out[t + 1] = KD ? tg : tg - a.id_offset;
                     if (a.trace) a.trace[t + 1] = forced ? INFINITY : key_dist(g);
                 }
             }
@@ -1267,6 +1277,9 @@ __global__ void __launch_bounds__(kSmemThreads, 1) grid_sample_smem(GridSmemArgs
         atomicAdd(a.counters + 1, touched);
     }
 }
+
+// out[i] = idmap[out[i]] - id_offset: kd-line tags to original indices
+__global__ void map_tags(uint64_t* out, uint64_t k, const uint32_t* idmap, uint64_t id_offset);
 
 constexpr int kNoFit = -1;
 
@@ -1317,7 +1330,7 @@ int sample_grid_smem(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint
     uint64_t* slots;
     uint64_t* d_forced;
     unsigned long long* cnt;
-    const uint64_t nslots = 3 * G * (1 + D);
+    const uint64_t nslots = (G + 1) * leader_words<D>();
     if ((rc = sc.alloc(&d_cut, G + 1))) return rc;
     if ((rc = sc.alloc(&slots, nslots))) return rc;
     if ((rc = sc.alloc(&d_forced, n_forced))) return rc;
@@ -1356,6 +1369,12 @@ int sample_grid_smem(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint
     timer.begin(stream);
     if ((rc = launch_persistent(kern, (int)G, kSmemThreads, args, smem, stream, G > 1))) return rc;
     timer.end(stream);
+    if (kd) {
+        stats_count_launch();
+        map_tags<<<(unsigned)std::min<uint64_t>((k + 255) / 256, 4096), 256, 0, stream>>>(
+            d_out, k, bt.idsnap, id_offset);
+        FPSGPU_CUDA_TRY(cudaGetLastError());
+    }
     unsigned long long h_cnt[2] = {0, 0};
     FPSGPU_CUDA_TRY(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, stream));
     if ((rc = check_device_error(bt.err, stream))) return rc;
@@ -1381,10 +1400,11 @@ int sample_grid(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint32_t 
     if ((rc = sc.alloc(&pkey, nkeys))) return rc;
     // grid: about two pieces per warp (pieces hold ~kPiece/2..kPiece points)
     uint64_t G = (points_in_range / (kPiece / 2) + 63) / 64;
-    G = std::max<uint64_t>(1, std::min<uint64_t>(G, (uint64_t)sms));
+    G = std::max<uint64_t>(1, std::min<uint64_t>({G, (uint64_t)sms, (uint64_t)kMaxGridCoords}));
     uint64_t* slots;
-    if ((rc = sc.alloc(&slots, 3 * G))) return rc;
-    FPSGPU_CUDA_TRY(cudaMemsetAsync(slots, 0, 3 * G * sizeof(uint64_t), stream));
+    const uint64_t nslots = (G + 1) * leader_words<0>();
+    if ((rc = sc.alloc(&slots, nslots))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemsetAsync(slots, 0, nslots * sizeof(uint64_t), stream));
     uint64_t* d_forced;
     if ((rc = sc.alloc(&d_forced, n_forced))) return rc;
     FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_forced, h_forced, n_forced * sizeof(uint64_t),
@@ -1421,6 +1441,12 @@ int sample_grid(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint32_t 
     const void* kern = kd ? (const void*)fps_sample<D, FMA, true> : (const void*)fps_sample<D, FMA, false>;
     if ((rc = launch_persistent(kern, (int)G, kSampleThreads, args, 0, stream, G > 1))) return rc;
     timer.end(stream);
+    if (kd) {
+        stats_count_launch();
+        map_tags<<<(unsigned)std::min<uint64_t>((k + 255) / 256, 4096), 256, 0, stream>>>(
+            d_out, k, bt.idsnap, id_offset);
+        FPSGPU_CUDA_TRY(cudaGetLastError());
+    }
     unsigned long long h_cnt[2] = {0, 0};
     FPSGPU_CUDA_TRY(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, stream));
     if ((rc = check_device_error(bt.err, stream))) return rc;

@@ -256,4 +256,138 @@ __device__ __forceinline__ uint64_t exchange_max_coords(uint64_t* slots, int G, 
     return g;
 }
 
+__device__ __forceinline__ uint64_t tagged(uint32_t tag, uint32_t payload) {
+    return ((uint64_t)tag << 32) | payload;
+}
+
+// Words per exchange record: key (two tagged halves) + D tagged coordinates,
+// padded to an even count for 16-byte loads.
+template <int D>
+constexpr int leader_words() { return (2 + D + 1) & ~1; }
+
+__device__ __forceinline__ void ld_relaxed_gpu_v2(const uint64_t* p, uint64_t& a, uint64_t& b) {
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
+}
+
+// Cross-CTA argmax through a leader (CTA 0), for persistent cooperative grids.
+// Called by ONE full warp per CTA, once per round; returns the winning key and
+// (D > 0) the winner's coordinates in win_c, identical in every CTA.
+//
+// Every 64-bit word written here carries the round tag (round + 1) in its high
+// half, and aligned 64-bit accesses are single-copy atomic, so a word showing
+// this round's tag holds this round's payload: no fences or clearing needed.
+//   1. every CTA writes its record (key hi, key lo, coordinates) into its slot;
+//   2. CTA 0 polls all G slots until they show the tag, takes the max and
+//      writes the winner's record into `bcast`;
+//   3. every CTA polls `bcast` until it shows the tag.
+// One slot row and one broadcast record suffice: a CTA rewrites its slot for
+// round t+1 only after reading the round-t broadcast, which CTA 0 writes only
+// after it has read every round-t slot; CTA 0 rewrites the broadcast for round
+// t+1 only after every CTA has published round t+1, i.e. after every CTA has
+// read the round-t broadcast.  L2 traffic per round is O(G) (the gather plus
+// one record per CTA), not the O(G^2) of an all-to-all poll.
+// Every poll loop gives up after kSpinLimit rounds: err is set, 0 returned.
+template <int D>
+__device__ __forceinline__ uint64_t exchange_leader(uint64_t* slots, uint64_t* bcast, int G,
+                                                    uint32_t round, uint64_t my_key,
+                                                    const float* my_c, float* win_c, int* err) {
+    constexpr int SW = leader_words<D>();
+    constexpr int kPer = kMaxGridCoords / 32;
+    const int lane = threadIdx.x & 31;
+    const uint32_t rt = round + 1u;
+    my_key |= kKeyValid;
+    if (lane == 0) {
+        uint64_t* mine = slots + (uint64_t)blockIdx.x * SW;
+        st_relaxed_gpu(mine + 0, tagged(rt, (uint32_t)(my_key >> 32)));
+        st_relaxed_gpu(mine + 1, tagged(rt, (uint32_t)my_key));
+#pragma unroll
+        for (int d = 0; d < D; ++d) st_relaxed_gpu(mine + 2 + d, tagged(rt, __float_as_uint(my_c[d])));
+    }
+    bool ok = true;
+    if (blockIdx.x == 0) {
+        uint64_t best = 0;
+        float bc[D > 0 ? D : 1];
+#pragma unroll
+        for (int d = 0; d < (D > 0 ? D : 1); ++d) bc[d] = 0.0f;
+        unsigned done = 0;
+        long long spins = 0;
+        for (;;) {
+#pragma unroll
+            for (int i = 0; i < kPer; ++i) {
+                const int j = lane + 32 * i;
+                if (j < G && !((done >> i) & 1u)) {
+                    uint64_t w[SW];
+#pragma unroll
+                    for (int k = 0; k < SW; k += 2) ld_relaxed_gpu_v2(slots + (uint64_t)j * SW + k, w[k], w[k + 1]);
+                    bool good = true;
+#pragma unroll
+                    for (int k = 0; k < 2 + D; ++k) good &= (uint32_t)(w[k] >> 32) == rt;
+                    if (good) {
+                        done |= 1u << i;
+                        const uint64_t key = ((uint64_t)(uint32_t)w[0] << 32) | (uint32_t)w[1];
+                        if (key > best) {
+                            best = key;
+#pragma unroll
+                            for (int d = 0; d < D; ++d) bc[d] = __uint_as_float((uint32_t)w[2 + d]);
+                        }
+                    }
+                }
+            }
+            bool all = true;
+#pragma unroll
+            for (int i = 0; i < kPer; ++i)
+                if (lane + 32 * i < G && !((done >> i) & 1u)) all = false;
+            if (__all_sync(kFull, all)) break;
+            if (++spins > kSpinLimit) {
+                ok = false;
+                break;
+            }
+        }
+        if (__all_sync(kFull, ok)) {
+            const uint64_t g = warp_max_key(best);
+            const int owner = __ffs(__ballot_sync(kFull, best == g)) - 1;
+            float wc[D > 0 ? D : 1];
+#pragma unroll
+            for (int d = 0; d < D; ++d) wc[d] = __shfl_sync(kFull, bc[d], owner);
+            if (lane == 0) {
+#pragma unroll
+                for (int d = 0; d < D; ++d) st_relaxed_gpu(bcast + 2 + d, tagged(rt, __float_as_uint(wc[d])));
+                st_relaxed_gpu(bcast + 1, tagged(rt, (uint32_t)g));
+                st_relaxed_gpu(bcast + 0, tagged(rt, (uint32_t)(g >> 32)));
+            }
+        } else {
+            ok = false;
+        }
+    }
+    // every CTA reads the broadcast record
+    uint64_t w[SW];
+#pragma unroll
+    for (int k = 0; k < SW; ++k) w[k] = 0;
+    if (lane == 0 && ok) {
+        long long spins = 0;
+        for (;;) {
+#pragma unroll
+            for (int k = 0; k < SW; k += 2) ld_relaxed_gpu_v2(bcast + k, w[k], w[k + 1]);
+            bool good = true;
+#pragma unroll
+            for (int k = 0; k < 2 + D; ++k) good &= (uint32_t)(w[k] >> 32) == rt;
+            if (good) break;
+            if (++spins > kSpinLimit) {
+                ok = false;
+                break;
+            }
+        }
+    }
+    ok = __shfl_sync(kFull, ok ? 1 : 0, 0) != 0;
+    if (!ok) {
+        if (lane == 0) atomicOr(err, kErrExchangeTimeout);
+        return 0;
+    }
+    const uint32_t hi = __shfl_sync(kFull, (uint32_t)w[0], 0);
+    const uint32_t lo = __shfl_sync(kFull, (uint32_t)w[1], 0);
+#pragma unroll
+    for (int d = 0; d < D; ++d) win_c[d] = __uint_as_float(__shfl_sync(kFull, (uint32_t)w[2 + d], 0));
+    return ((uint64_t)hi << 32) | lo;
+}
+
 }  // namespace fpsgpu
