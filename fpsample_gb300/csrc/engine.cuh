@@ -702,17 +702,26 @@ __device__ __forceinline__ uint64_t recompute_piece(const float* xb, uint64_t xs
 
 // ---- batched sampling: one CTA per cloud -------------------------------------
 //
-// A persistent grid pulls clouds from a queue (largest first).  The CTA keeps
-// its cloud's piece records in shared memory: max key, bounding box, start and
-// the coordinates of the max point; clouds of at most `mcap` points also keep
-// their points (coordinates, running distance, tag) there.  One iteration is:
-// every warp tests its pieces against the reference point, recomputes the
-// dirty ones, and offers its best (key, piece); warp 0 picks the winner and
-// reads the next reference point from the winning piece's record.  Two
-// __syncthreads per sample, no cross-CTA communication, no global load for the
-// winner.
-// 1024 threads per cloud (fewer for D > 4, where 64 registers would spill)
-constexpr int batch_threads(int D) { return D <= 4 ? 1024 : 512; }
+// A persistent grid pulls clouds from a queue (largest first).  Every thread
+// owns up to batch_slots(D) pieces of the current cloud and keeps their boxes and
+// max keys in registers; piece q belongs to warp q % nwarps, so pieces that
+// are neighbours in storage order (and tend to turn dirty together) land in
+// different warps.  Clouds of at most `mcap` points keep their points
+// (coordinates, running distance, tag) in shared memory, larger ones read them
+// from L2/HBM.  One sample:
+//   1. every thread tests its pieces against the reference point r (registers
+//      only); a warp recomputes its dirty pieces one after the other
+//      (recompute_piece: one round trip each);
+//   2. each warp offers its best key and that piece's max coordinates in a
+//      parity-double-buffered shared array; one __syncthreads;
+//   3. every warp reduces the 32 offers itself and takes the winner's
+//      coordinates as the next r -- no second barrier, no global load.
+// kd-line outputs hold tags while sampling and are mapped to original indices
+// by the CTA after the cloud's last sample.
+// threads per cloud and pieces per thread: 2048 pieces per cloud either way;
+// 512 threads x 4 slots for D >= 3 keeps the registers from spilling
+constexpr int batch_threads(int D) { return D <= 2 ? 1024 : 512; }
+constexpr int batch_slots(int D) { return 2048 / batch_threads(D); }
 
 struct BatchArgs {
     const float* X;             // SoA [D][n], storage order (all clouds)
@@ -734,31 +743,28 @@ struct BatchArgs {
     uint64_t* out;
     unsigned int* queue;
     unsigned long long* counters;
-    uint32_t cap;               // piece records that fit in shared memory
+    uint32_t cap;               // pieces per cloud at most (batch_slots(D) x threads)
     uint32_t mcap;              // points that fit in shared memory
 };
 
 inline size_t batch_smem_bytes(int D, uint32_t cap, uint32_t mcap) {
-    return (size_t)cap * (8 + 12 * D) + (size_t)(cap + 1) * 4 + (size_t)mcap * (4 * D + 8) + 16;
+    return (size_t)(cap + 1) * 4 + (size_t)cap * D * 4 + (size_t)mcap * (4 * D + 8) + 16;
 }
 
 template <int D, bool FMA, bool KD>
 __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
-    __shared__ uint64_t s_wkey[32];
-    __shared__ uint32_t s_wq[32];
-    __shared__ float s_ref[kMaxDim];
+    __shared__ uint64_t s_wkey[2][32];
+    __shared__ float s_wc[2][32][kMaxDim];
     __shared__ uint32_t s_item;
     const uint32_t cap = a.cap, mcap = a.mcap;
-    uint64_t* s_key = reinterpret_cast<uint64_t*>(s_dyn);
-    float* s_lo = reinterpret_cast<float*>(s_key + cap);  // [D][cap]
-    float* s_hi = s_lo + (size_t)D * cap;
-    float* s_mc = s_hi + (size_t)D * cap;                 // coordinates of each piece's max
-    float* s_x = s_mc + (size_t)D * cap;                  // [D][mcap]
-    float* s_dis = s_x + (size_t)D * mcap;                // [mcap]
+    float* s_x = reinterpret_cast<float*>(s_dyn);                 // [D][mcap]
+    float* s_dis = s_x + (size_t)D * mcap;                        // [mcap]
     uint32_t* s_tag = reinterpret_cast<uint32_t*>(s_dis + mcap);  // [mcap]
-    uint32_t* s_ps = s_tag + mcap;                        // [cap + 1] local piece starts
+    uint32_t* s_ps = s_tag + mcap;                                // [cap + 1] local piece starts
+    float* s_mc = reinterpret_cast<float*>(s_ps + cap + 1);       // [D][cap] max coordinates
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const uint32_t T = blockDim.x;
     const uint64_t n = a.n;
     unsigned long long tested = 0, touched = 0;
 
@@ -775,18 +781,25 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
         const uint32_t nc = (uint32_t)(a.cloud_off[c + 1] - coff);
         const uint64_t ooff = a.out_off[c];
         const bool resident = nc <= mcap;
-        for (uint32_t i = tid; i <= np; i += blockDim.x) {
-            s_ps[i] = a.pstart[P0 + i] - (uint32_t)coff;
-            if (i < np) {
+
+        // my pieces: slot j holds piece j * T + lane * nwarps + warp
+        float lo[batch_slots(D)][D], hi[batch_slots(D)][D];
+        uint64_t key[batch_slots(D)];
+        uint32_t myq[batch_slots(D)];
 #pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    s_lo[(size_t)d * cap + i] = a.plo[(uint64_t)(P0 + i) * D + d];
-                    s_hi[(size_t)d * cap + i] = a.phi[(uint64_t)(P0 + i) * D + d];
-                }
+        for (int j = 0; j < batch_slots(D); ++j) {
+            myq[j] = (uint32_t)j * T + (uint32_t)lane * nwarps + warp;
+            key[j] = 0;
+            const bool have = myq[j] < np;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                lo[j][d] = have ? a.plo[(uint64_t)(P0 + myq[j]) * D + d] : 0.0f;
+                hi[j][d] = have ? a.phi[(uint64_t)(P0 + myq[j]) * D + d] : 0.0f;
             }
         }
+        for (uint32_t i = tid; i <= np; i += T) s_ps[i] = a.pstart[P0 + i] - (uint32_t)coff;
         if (resident) {
-            for (uint32_t i = tid; i < nc; i += blockDim.x) {
+            for (uint32_t i = tid; i < nc; i += T) {
 #pragma unroll
                 for (int d = 0; d < D; ++d) s_x[(size_t)d * mcap + i] = a.X[(uint64_t)d * n + coff + i];
                 s_tag[i] = a.tag[coff + i];
@@ -797,86 +810,81 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
         float* disb = resident ? s_dis : a.dis + coff;
         const uint32_t* tagb = resident ? s_tag : a.tag + coff;
         const uint32_t tag0 = (uint32_t)a.cloud_tag0[c];
-        if (tid < D) s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
-        // outputs hold tags while sampling (kd-line tags become original
-        // indices after the loop, off the per-sample critical path)
+        float r[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) r[d] = a.Xref[(uint64_t)d * n + tag0];
+        // outputs hold tags while sampling (kd-line tags are mapped at the end)
         if (tid == 0 && K > 0) a.out[ooff] = KD ? tag0 : tag0 - coff;
         __syncthreads();
-        const uint32_t stride = 32u * nwarps;  // piece q belongs to warp q % nwarps
 
+        int par = 0;
         for (uint64_t t = 0; t + 1 < K; ++t) {
-            float r[D];
-#pragma unroll
-            for (int d = 0; d < D; ++d) r[d] = s_ref[d];
             uint64_t best = 0;
             uint32_t bestq = 0;
-            for (uint32_t qb = 0; qb < np; qb += stride) {
-                const uint32_t q = qb + lane * nwarps + warp;
-                const bool have = q < np;
-                const uint32_t hb = __ballot_sync(kFull, have);
-                if (t > 0 && lane == 0) tested += __popc(hb);
-                uint64_t key = have && t > 0 ? s_key[q] : 0ull;
-                bool dirty = have;
-                if (have && t > 0) {
-                    float lo[D], hi[D];
 #pragma unroll
-                    for (int d = 0; d < D; ++d) {
-                        lo[d] = s_lo[(size_t)d * cap + q];
-                        hi[d] = s_hi[(size_t)d * cap + q];
-                    }
-                    dirty = box_bound<D, FMA>(lo, hi, r) < key_dist(key);
+            for (int j = 0; j < batch_slots(D); ++j) {
+                const bool have = myq[j] < np;
+                bool dirty = have;
+                if (t > 0) {
+                    tested += have ? 1u : 0u;
+                    dirty = have && box_bound<D, FMA>(lo[j], hi[j], r) < key_dist(key[j]);
                 }
                 uint32_t m = __ballot_sync(kFull, dirty);
                 while (m) {
                     const int l = __ffs(m) - 1;
                     m &= m - 1;
-                    const uint32_t qq = qb + l * nwarps + warp;
-                    const uint32_t ps = s_ps[qq], pe = s_ps[qq + 1];
-                    touched += pe - ps;
+                    const uint32_t q = __shfl_sync(kFull, myq[j], l);
+                    const uint32_t ps = s_ps[q], pe = s_ps[q + 1];
+                    if (lane == 0) touched += pe - ps;
                     float pc[D];
                     const uint64_t wk =
                         recompute_piece<D, FMA, KD>(xb, xs, disb, tagb, ps, pe, r, t == 0, pc);
                     if (lane == l) {
-                        key = wk;
-                        s_key[qq] = wk;
+                        key[j] = wk;
 #pragma unroll
-                        for (int d = 0; d < D; ++d) s_mc[(size_t)d * cap + qq] = pc[d];
+                        for (int d = 0; d < D; ++d) s_mc[(size_t)d * cap + q] = pc[d];
                     }
                 }
-                if (have && key > best) {
-                    best = key;
-                    bestq = q;
+                if (have && key[j] > best) {
+                    best = key[j];
+                    bestq = myq[j];
                 }
             }
+            // the warp's offer: best key and its piece's max coordinates
             const uint64_t wb = warp_max_key(best);
-            const int wl = __ffs(__ballot_sync(kFull, best == wb)) - 1;
-            bestq = __shfl_sync(kFull, bestq, wl);
-            if (lane == 0) {
-                s_wkey[warp] = wb;
-                s_wq[warp] = bestq;
-            }
+            const int owner = __ffs(__ballot_sync(kFull, best == wb)) - 1;
+            const uint32_t qw = __shfl_sync(kFull, bestq, owner);
+            if (lane < D) s_wc[par][warp][lane] = wb ? s_mc[(size_t)lane * cap + qw] : 0.0f;
+            if (lane == 0) s_wkey[par][warp] = wb;
             __syncthreads();
-            if (warp == 0) {
-                const uint64_t kw = lane < nwarps ? s_wkey[lane] : 0ull;
-                const uint64_t g = warp_max_key(kw);
-                const int w = __ffs(__ballot_sync(kFull, lane < nwarps && kw == g)) - 1;
-                const uint32_t qwin = s_wq[w];
-                if (lane < D) s_ref[lane] = s_mc[(size_t)lane * cap + qwin];
-                if (lane == 0) {
-                    const uint32_t tg = key_pos<KD>(g);
-                    a.out[ooff + t + 1] = KD ? tg : tg - coff;
-                }
+            // every warp picks the winner itself
+            const uint64_t kw = lane < nwarps ? s_wkey[par][lane] : 0ull;
+            const uint64_t g = warp_max_key(kw);
+            const int w = __ffs(__ballot_sync(kFull, lane < nwarps && kw == g)) - 1;
+#pragma unroll
+            for (int d = 0; d < D; ++d) r[d] = s_wc[par][w][d];
+            if (tid == 0) {
+                const uint32_t tg = key_pos<KD>(g);
+                a.out[ooff + t + 1] = KD ? tg : tg - coff;
             }
-            __syncthreads();
+            par ^= 1;
         }
+        __syncthreads();  // thread 0's output writes are visible to the CTA
         if (KD) {
-            for (uint64_t i = tid; i < K; i += blockDim.x)
-                a.out[ooff + i] = a.idmap[a.out[ooff + i]] - coff;
+            for (uint64_t i = tid; i < K; i += T) a.out[ooff + i] = a.idmap[a.out[ooff + i]] - coff;
         }
     }
-    if (a.counters && lane == 0) {
-        atomicAdd(a.counters, tested);
-        atomicAdd(a.counters + 1, touched);
+    if (a.counters) {
+        // warp sums, one atomic per warp
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            tested += __shfl_xor_sync(kFull, tested, o);
+            touched += __shfl_xor_sync(kFull, touched, o);
+        }
+        if (lane == 0) {
+            atomicAdd(a.counters, tested);
+            atomicAdd(a.counters + 1, touched);
+        }
     }
 }
 
@@ -1562,8 +1570,7 @@ int run_batch(const BatchCall& bc) {
     FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
     FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     const size_t avail = (size_t)smem_optin - 1024;  // static shared memory
-    const size_t rec = sizeof(uint64_t) + 3 * D * sizeof(float) + sizeof(uint32_t);
-    const uint32_t cap_max = (uint32_t)(avail / 2 / rec);
+    const uint32_t cap_max = (uint32_t)batch_slots(D) * batch_threads(D);
     std::vector<uint64_t> out_off(C), tag0(C);
     std::vector<uint32_t> small, big;
     uint64_t acc = 0;
@@ -1629,7 +1636,8 @@ int run_batch(const BatchCall& bc) {
         a.queue = d_queue;
         a.counters = cnt;
         a.cap = cap;
-        // what the piece records leave of shared memory holds small clouds' points
+        // what the piece starts and max coordinates leave of shared memory holds
+        // small clouds' points
         uint64_t max_nc = 0;
         for (uint32_t c : small) max_nc = std::max<uint64_t>(max_nc, bc.off[c + 1] - bc.off[c]);
         const size_t left = avail - batch_smem_bytes(D, cap, 0);
