@@ -1313,7 +1313,9 @@ int sample_grid_smem(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint
     int dev = 0, smem_max = 0;
     FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
     FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const size_t budget = (size_t)smem_max - 1024;  // static shared memory
+    cudaFuncAttributes fa{};
+    FPSGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)grid_sample_smem<D, FMA, true>));
+    const size_t budget = (size_t)smem_max - fa.sharedSizeBytes - 256;
     uint64_t G = std::min<uint64_t>({(uint64_t)sms, (uint64_t)kMaxGridCoords,
                                      std::max<uint64_t>(1, pts / 2048)});
     // cut the piece range at the pieces nearest to equal point shares
@@ -1569,7 +1571,13 @@ int run_batch(const BatchCall& bc) {
     int dev = 0, smem_optin = 0;
     FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
     FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const size_t avail = (size_t)smem_optin - 1024;  // static shared memory
+    size_t static_smem = 0;
+    {
+        cudaFuncAttributes fa{};
+        FPSGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)batch_sample<D, FMA, true>));
+        static_smem = fa.sharedSizeBytes;
+    }
+    const size_t avail = (size_t)smem_optin - static_smem - 256;
     const uint32_t cap_max = (uint32_t)batch_slots(D) * batch_threads(D);
     std::vector<uint64_t> out_off(C), tag0(C);
     std::vector<uint32_t> small, big;

@@ -15,12 +15,16 @@ namespace fpsgpu {
 int set_error(int code, const char* fmt, ...);
 void clear_error();
 
+// On failure the error is also taken off the runtime's last-error slot, so a
+// later, unrelated cudaGetLastError() does not report it again.
 #define FPSGPU_CUDA_TRY(expr)                                                              \
     do {                                                                                   \
         cudaError_t e_ = (expr);                                                           \
-        if (e_ != cudaSuccess)                                                             \
+        if (e_ != cudaSuccess) {                                                           \
+            (void)cudaGetLastError();                                                      \
             return ::fpsgpu::set_error(FPSGPU_ERR_CUDA, "%s failed: %s (%s:%d)", #expr,    \
                                        cudaGetErrorString(e_), __FILE__, __LINE__);        \
+        }                                                                                  \
     } while (0)
 
 // Properties of the current device plus the library's own stream on it.
