@@ -405,6 +405,51 @@ def run_gpu_arm(args):
         dist.destroy_process_group()
 
 
+def run_latency_probe(args):
+    """Per-sample latency of one cloud at a time (not the headline metric):
+    uniform box clouds, D=3, K=N/4, timed end to end (build + sampling) through
+    the batched entry point with one cloud and through the single-cloud entry
+    point; plus the gmm-1m workload (kd-line h=7 and vanilla, K=16384)."""
+    import torch
+
+    from fpsample_gb300 import capi
+    from fpsample_gb300 import workloads as W
+
+    def best_of(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
+    res = {}
+    rng = np.random.default_rng(0)
+    s = torch.cuda.current_stream().cuda_stream
+    for n in (4096, 16384, 32768, 65536, 124000):
+        p = (rng.random((n, 3)) * rng.uniform(0.1, 10, 3)).astype(np.float32)
+        t = torch.from_numpy(p).cuda()
+        k = n // 4
+        h = h_for(n)
+        out = torch.empty(k, dtype=torch.int64, device="cuda")
+        dt = best_of(lambda: capi.kdline_batch_device(t.data_ptr(), [0, n], 3, [k], [h], [0],
+                                                      out.data_ptr(), s))
+        res[f"batched_one_cloud_n{n}"] = {"ms": dt * 1e3, "us_per_sample": dt * 1e6 / k}
+        dt = best_of(lambda: capi.kdline_device(t.data_ptr(), n, 3, k, 0, h, out.data_ptr(), 0, s))
+        res[f"single_cloud_n{n}"] = {"ms": dt * 1e3, "us_per_sample": dt * 1e6 / k}
+    g = torch.from_numpy(W.gmm_cloud(1 << 20, seed=W.SEEDS["gmm-1m"])).cuda()
+    out = torch.empty(16384, dtype=torch.int64, device="cuda")
+    dt = best_of(lambda: capi.kdline_device(g.data_ptr(), 1 << 20, 3, 16384, 0, 7, out.data_ptr(), 0, s))
+    res["gmm1m_kdline_h7"] = {"ms": dt * 1e3, "us_per_sample": dt * 1e6 / 16384}
+    dt = best_of(lambda: capi.fps_device(g.data_ptr(), 1 << 20, 3, 16384, [0], out.data_ptr(), 0, s))
+    res["gmm1m_vanilla"] = {"ms": dt * 1e3, "us_per_sample": dt * 1e6 / 16384}
+    print(json.dumps({"probe": "latency", "results": res}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -413,9 +458,14 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched-256",
                     choices=["batched-256", "gmm-1m", "single-4k"])
+    ap.add_argument("--probe", default=None, choices=["latency"],
+                    help="print a diagnostic table instead of the benchmark line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.probe == "latency":
+        run_latency_probe(args)
+        return
     if args.impl == "reference":
         run_reference_arm(args)
     else:
