@@ -405,6 +405,60 @@ def run_gpu_arm(args):
         dist.destroy_process_group()
 
 
+def run_served(args):
+    """configs[3]: a Poisson stream of requests (2000/s) into the request server.
+    The first --served-window seconds of the 10 s stream are replayed at their
+    arrival times (the full stream would need ~80 GB of host memory for its
+    points).  Reports completed requests/s over the replay, the latency
+    percentiles (submit to result), and the same for requests of <= 65536
+    points; a sample of results is compared with one call per cloud."""
+    import threading
+
+    from fpsample_gb300 import capi
+    from fpsample_gb300 import workloads as W
+
+    reqs = list(W.request_stream(rate=2000.0, duration_s=args.served_window,
+                                 seed=W.SEEDS["served"]))
+    reqs = [(r.arrival_s, r.points, r.k, h_for(r.points.shape[0]), r.start) for r in reqs]
+    with capi.Server(150 << 30, small_workers=args.small_workers,
+                     large_workers=args.large_workers) as srv:
+        for a, p, k, h, s in reqs[: min(8, len(reqs))]:  # warm-up (not timed)
+            srv.result(srv.submit(p, k, h, s))
+        tickets = [None] * len(reqs)
+        t0 = time.perf_counter()
+        for i, (a, p, k, h, s) in enumerate(reqs):
+            dt = t0 + a - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            tickets[i] = srv.submit(p, k, h, s)
+        res = [srv.result(t) for t in tickets]
+        wall = time.perf_counter() - t0
+    lat = np.array([r[2] for r in res])
+    queue = np.array([r[1] for r in res])
+    small = np.array([p.shape[0] <= 65536 for _, p, _, _, _ in reqs])
+    check = list(range(0, len(reqs), max(1, len(reqs) // 8)))
+    same = all(np.array_equal(res[i][0], capi.bucket_fps_kdline(reqs[i][1], reqs[i][2],
+                                                                 reqs[i][4], reqs[i][3]))
+               for i in check)
+    pct = lambda x, q: float(np.percentile(x, q)) if len(x) else None
+    line = {
+        "metric": "requests/sec (served)", "value": len(reqs) / wall, "unit": "requests/s",
+        "n_gpus": 1, "higher_is_better": True, "data": "synthetic (seeded generators)",
+        "config": {"workload": "served", "offered_rate_per_s": 2000, "window_s": args.served_window,
+                   "requests": len(reqs), "points_total": int(sum(p.shape[0] for _, p, _, _, _ in reqs)),
+                   "samples_total": int(sum(k for _, _, k, _, _ in reqs)),
+                   "small_workers": args.small_workers, "large_workers": args.large_workers,
+                   "memory_budget_gb": 150},
+        "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max())},
+        "latency_ms_n_le_65536": {"p50": pct(lat[small], 50), "p99": pct(lat[small], 99),
+                                  "count": int(small.sum())},
+        "queue_ms": {"p50": pct(queue, 50), "p99": pct(queue, 99)},
+        "samples_per_s": sum(k for _, _, k, _, _ in reqs) / wall,
+        "wall_s": wall, "identical_to_single_calls": same, "checked": check,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_latency_probe(args):
     """Per-sample latency of one cloud at a time (not the headline metric):
     uniform box clouds, D=3, K=N/4, timed end to end (build + sampling) through
@@ -457,7 +511,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched-256",
-                    choices=["batched-256", "gmm-1m", "single-4k"])
+                    choices=["batched-256", "gmm-1m", "single-4k", "served"])
+    ap.add_argument("--served-window", type=float, default=0.1,
+                    help="seconds of the served request stream to replay")
+    ap.add_argument("--small-workers", type=int, default=8)
+    ap.add_argument("--large-workers", type=int, default=2)
     ap.add_argument("--probe", default=None, choices=["latency"],
                     help="print a diagnostic table instead of the benchmark line")
     args = ap.parse_args()
@@ -465,6 +523,9 @@ def main():
         args.warmup = 3
     if args.probe == "latency":
         run_latency_probe(args)
+        return
+    if args.workload == "served" and args.impl != "reference":
+        run_served(args)
         return
     if args.impl == "reference":
         run_reference_arm(args)

@@ -30,6 +30,11 @@ SIGNATURES = {
     "fpsgpu_kdline_build": (ctypes.c_int, [_f32p, _sz, _sz, _sz, _u64p, _u64p, _szp]),
     "fpsgpu_kdline_batch": (ctypes.c_int, [_f32p, _szp, _sz, _sz, _szp, _szp, _szp, _szp]),
     "fpsgpu_kdline_batch_device": (ctypes.c_int, [_vp, _szp, _sz, _sz, _szp, _szp, _szp, _vp, _vp]),
+    "fpsgpu_server_create": (ctypes.c_int, [_sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)]),
+    "fpsgpu_server_submit": (ctypes.c_int, [_vp, _f32p, _sz, _sz, _sz, _sz, _sz, _szp, _u64p]),
+    "fpsgpu_server_wait": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_double)]),
+    "fpsgpu_server_destroy": (ctypes.c_int, [_vp]),
     "fpsgpu_set_fp_mode": (ctypes.c_int, [ctypes.c_int]),
     "fpsgpu_get_fp_mode": (ctypes.c_int, []),
     "fpsgpu_stats_reset": (None, []),
@@ -230,3 +235,50 @@ def fps_device_noalloc(points_ptr: int, n: int, dim: int, n_samples: int, starts
     rc = lib().fpsgpu_fps_device_noalloc(points_ptr, n, dim, n_samples, st.ctypes.data_as(_szp),
                                          st.size, out_ptr, trace_ptr or None, stream or None)
     _check("fpsgpu_fps_device_noalloc", rc)
+
+
+class Server:
+    """QuickFPS request server with continuous batching (fpsgpu_server_*).
+
+    submit() returns a ticket immediately; result(ticket) blocks and returns
+    (indices, queue_ms, total_ms).  Indices equal bucket_fps_kdline_sampling's.
+    """
+
+    def __init__(self, max_device_bytes: int = 150 << 30, small_workers: int = 8,
+                 large_workers: int = 2):
+        h = _vp()
+        _check("fpsgpu_server_create",
+               lib().fpsgpu_server_create(max_device_bytes, small_workers, large_workers,
+                                          ctypes.byref(h)))
+        self._h = h
+        self._live = {}
+
+    def submit(self, pc, n_samples: int, height: int, start_idx: int = 0) -> int:
+        a = _rows(pc)
+        out = np.empty(n_samples, np.uint64)
+        t = ctypes.c_uint64(0)
+        _check("fpsgpu_server_submit",
+               lib().fpsgpu_server_submit(self._h, a.ctypes.data_as(_f32p), a.shape[0], a.shape[1],
+                                          n_samples, start_idx, height, out.ctypes.data_as(_szp),
+                                          ctypes.byref(t)))
+        self._live[t.value] = (a, out)  # keep the buffers alive until the result is taken
+        return t.value
+
+    def result(self, ticket: int):
+        q = ctypes.c_double(0)
+        tot = ctypes.c_double(0)
+        rc = lib().fpsgpu_server_wait(self._h, ticket, ctypes.byref(q), ctypes.byref(tot))
+        _, out = self._live.pop(ticket)
+        _check("fpsgpu_server_wait", rc)
+        return out, q.value, tot.value
+
+    def close(self) -> None:
+        if self._h:
+            lib().fpsgpu_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

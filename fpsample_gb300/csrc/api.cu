@@ -479,6 +479,17 @@ int bucket_fps_kdline(const float* raw_data, size_t n_points, size_t dim, size_t
 int fpsgpu_kdline_batch_device(const float* d_points, const size_t* h_offsets, size_t n_clouds,
                                size_t dim, const size_t* h_n_samples, const size_t* h_start_idx,
                                const size_t* h_height, uint64_t* d_out, void* stream) {
+    return fpsgpu::kdline_batch_device_capped(d_points, h_offsets, n_clouds, dim, h_n_samples,
+                                              h_start_idx, h_height, d_out, stream, 0);
+}
+
+}  // extern "C"
+
+namespace fpsgpu {
+int kdline_batch_device_capped(const float* d_points, const size_t* h_offsets, size_t n_clouds,
+                               size_t dim, const size_t* h_n_samples, const size_t* h_start_idx,
+                               const size_t* h_height, uint64_t* d_out, void* stream,
+                               int max_grid) {
     clear_error();
     if (n_clouds == 0) return FPSGPU_OK;
     if (!h_offsets || !h_n_samples || !h_start_idx || !h_height)
@@ -508,9 +519,12 @@ int fpsgpu_kdline_batch_device(const float* d_points, const size_t* h_offsets, s
     b.kd = true;
     b.d_out = d_out;
     b.stream = s;
-    b.sms = ctx.sms;
+    b.sms = max_grid > 0 && max_grid < ctx.sms ? max_grid : ctx.sms;
     return fp_mode() == FPSGPU_FP_FMA ? run_batch_fma((int)dim, b) : run_batch_nofma((int)dim, b);
 }
+}  // namespace fpsgpu
+
+extern "C" {
 
 int fpsgpu_kdline_batch(const float* raw_data, const size_t* offsets, size_t n_clouds, size_t dim,
                         const size_t* n_samples, const size_t* start_idx, const size_t* height,

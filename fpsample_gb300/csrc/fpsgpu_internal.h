@@ -87,6 +87,14 @@ int run_engine_fma(int dim, const EngineCall& c);
 int run_batch_nofma(int dim, const BatchCall& c);
 int run_batch_fma(int dim, const BatchCall& c);
 
+// fpsgpu_kdline_batch_device with the multi-CTA samplers (clouds too large for
+// one CTA) limited to max_grid CTAs (0: all SMs), so that several batches can
+// share the GPU.
+int kdline_batch_device_capped(const float* d_points, const size_t* h_offsets, size_t n_clouds,
+                               size_t dim, const size_t* h_n_samples, const size_t* h_start_idx,
+                               const size_t* h_height, uint64_t* d_out, void* stream,
+                               int max_grid);
+
 // measurement counters (fpsgpu_stats_*)
 void stats_count_launch(uint64_t n = 1);
 bool stats_timing_enabled();

@@ -1,0 +1,273 @@
+// Request server: QuickFPS as a service with continuous batching.
+//
+// Clients submit one cloud per request (host buffers) at any time.  Worker
+// threads, each with its own CUDA stream, repeatedly take every request that is
+// waiting in their size class -- as long as it fits in the device-memory
+// budget -- and run them as one batch through the batched engine
+// (fpsgpu_kdline_batch_device); requests that arrive while a batch is on the
+// GPU are picked up by the next free worker, so work from different batches
+// overlaps on the device.  Each request's points, running distances and piece
+// state stay on the device until its K samples are done; then its indices are
+// copied back and the request completes.  Results are identical to one
+// bucket_fps_kdline call per request: the batched engine is exact per cloud.
+//
+// Size classes keep small requests from waiting behind very large ones:
+// requests of at most kSmallPoints points go to the "small" workers, the rest
+// to the "large" workers.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "fpsgpu_internal.h"
+
+namespace fpsgpu {
+namespace {
+
+constexpr size_t kSmallPoints = 262144;
+constexpr size_t kMaxBatch = 64;
+
+double now_ms() {
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+// Device bytes a request may need at peak: the input and the engine's scratch
+// (coordinates twice, tags, ids, partner scratch, flags, distances, pieces).
+size_t request_bytes(size_t n, size_t dim, size_t k) {
+    return n * (dim * 4 * 3 + 4 * 6 + 1) + k * 8 + (n / 32 + 1024) * (8 * dim + 16) + (1u << 16);
+}
+
+struct Request {
+    uint64_t id = 0;
+    const float* pts = nullptr;
+    size_t n = 0, dim = 0, k = 0, start = 0, height = 0;
+    uint64_t* out = nullptr;
+    size_t bytes = 0;
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    int rc = 0;
+    bool done = false;
+};
+
+}  // namespace
+
+struct Server {
+    int device = 0;
+    size_t budget = 0, in_use = 0;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request*> pending[2];  // [0] small, [1] large
+    std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
+    uint64_t next_id = 1;
+    bool stopping = false;
+    std::vector<std::thread> workers;
+    std::atomic<uint64_t> batches{0};
+    int grid_cap = 0;  // CTAs a multi-CTA sampler may use, so batches can overlap
+
+    void worker(int cls) {
+        cudaSetDevice(device);
+        cudaStream_t stream;
+        if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return;
+        float* h_pts = nullptr;
+        uint64_t* h_out = nullptr;
+        size_t cap_pts = 0, cap_out = 0;
+        for (;;) {
+            std::vector<Request*> batch;
+            size_t bytes = 0;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv_work.wait(lk, [&] { return stopping || !pending[cls].empty(); });
+                if (stopping && pending[cls].empty()) break;
+                // admit in arrival order while the memory budget allows; a
+                // request larger than the whole budget still runs alone
+                while (!pending[cls].empty() && batch.size() < kMaxBatch) {
+                    Request* r = pending[cls].front();
+                    if (!batch.empty() && r->dim != batch[0]->dim) break;
+                    if (in_use + bytes + r->bytes > budget && !(in_use == 0 && batch.empty())) break;
+                    pending[cls].pop_front();
+                    bytes += r->bytes;
+                    batch.push_back(r);
+                }
+                if (batch.empty()) {  // nothing fits now: wait for memory to free up
+                    cv_done.wait(lk);
+                    continue;
+                }
+                in_use += bytes;
+                const double t = now_ms();
+                for (Request* r : batch) r->t_admit = t;
+            }
+            // pack the batch into pinned staging, one upload, one batched call
+            const size_t dim = batch[0]->dim;
+            std::vector<size_t> off(batch.size() + 1, 0), ks, starts, heights;
+            size_t ktot = 0;
+            for (size_t i = 0; i < batch.size(); ++i) {
+                off[i + 1] = off[i] + batch[i]->n;
+                ks.push_back(batch[i]->k);
+                starts.push_back(batch[i]->start);
+                heights.push_back(batch[i]->height);
+                ktot += batch[i]->k;
+            }
+            int rc = FPSGPU_OK;
+            const size_t npts = off.back();
+            if (npts * dim > cap_pts) {
+                if (h_pts) cudaFreeHost(h_pts);
+                cap_pts = npts * dim * 2;
+                if (cudaHostAlloc((void**)&h_pts, cap_pts * sizeof(float), cudaHostAllocDefault) != cudaSuccess) {
+                    h_pts = nullptr;
+                    cap_pts = 0;
+                    rc = set_error(FPSGPU_ERR_CUDA, "pinned staging allocation failed");
+                }
+            }
+            if (!rc && ktot > cap_out) {
+                if (h_out) cudaFreeHost(h_out);
+                cap_out = ktot * 2;
+                if (cudaHostAlloc((void**)&h_out, cap_out * sizeof(uint64_t), cudaHostAllocDefault) != cudaSuccess) {
+                    h_out = nullptr;
+                    cap_out = 0;
+                    rc = set_error(FPSGPU_ERR_CUDA, "pinned staging allocation failed");
+                }
+            }
+            float* d_pts = nullptr;
+            uint64_t* d_out = nullptr;
+            if (!rc) {
+                for (size_t i = 0; i < batch.size(); ++i)
+                    std::memcpy(h_pts + off[i] * dim, batch[i]->pts, batch[i]->n * dim * sizeof(float));
+                if (cudaMallocAsync((void**)&d_pts, npts * dim * sizeof(float), stream) != cudaSuccess ||
+                    cudaMallocAsync((void**)&d_out, ktot * sizeof(uint64_t), stream) != cudaSuccess)
+                    rc = set_error(FPSGPU_ERR_CUDA, "device allocation for a batch failed");
+            }
+            if (!rc && cudaMemcpyAsync(d_pts, h_pts, npts * dim * sizeof(float), cudaMemcpyHostToDevice,
+                                       stream) != cudaSuccess)
+                rc = set_error(FPSGPU_ERR_CUDA, "upload failed");
+            if (!rc)
+                rc = kdline_batch_device_capped(d_pts, off.data(), batch.size(), dim, ks.data(),
+                                                starts.data(), heights.data(), d_out, stream,
+                                                grid_cap);
+            if (!rc && cudaMemcpyAsync(h_out, d_out, ktot * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                                       stream) != cudaSuccess)
+                rc = set_error(FPSGPU_ERR_CUDA, "download failed");
+            if (d_pts) cudaFreeAsync(d_pts, stream);
+            if (d_out) cudaFreeAsync(d_out, stream);
+            if (cudaStreamSynchronize(stream) != cudaSuccess && !rc)
+                rc = set_error(FPSGPU_ERR_CUDA, "batch failed on the device");
+            batches.fetch_add(1);
+            {
+                size_t o = 0;
+                for (Request* r : batch) {
+                    if (!rc) std::memcpy(r->out, h_out + o, r->k * sizeof(uint64_t));
+                    o += r->k;
+                }
+                std::lock_guard<std::mutex> lk(mu);
+                const double t = now_ms();
+                for (Request* r : batch) {
+                    r->rc = rc;
+                    r->t_done = t;
+                    r->done = true;
+                }
+                in_use -= bytes;
+            }
+            cv_done.notify_all();
+            cv_work.notify_all();
+        }
+        if (h_pts) cudaFreeHost(h_pts);
+        if (h_out) cudaFreeHost(h_out);
+        cudaStreamDestroy(stream);
+    }
+};
+
+}  // namespace fpsgpu
+
+using fpsgpu::Request;
+using fpsgpu::Server;
+
+extern "C" {
+
+int fpsgpu_server_create(size_t max_device_bytes, int small_workers, int large_workers,
+                         void** out) {
+    fpsgpu::clear_error();
+    if (!out || small_workers < 1 || large_workers < 1)
+        return fpsgpu::set_error(FPSGPU_ERR_ARG, "need an output handle and >= 1 worker per class");
+    int dev = 0;
+    FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
+    auto* s = new Server();
+    s->device = dev;
+    s->budget = max_device_bytes;
+    int sms = 0;
+    FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    s->grid_cap = std::max(1, sms / (large_workers + 1));
+    for (int i = 0; i < small_workers; ++i) s->workers.emplace_back(&Server::worker, s, 0);
+    for (int i = 0; i < large_workers; ++i) s->workers.emplace_back(&Server::worker, s, 1);
+    *out = s;
+    return FPSGPU_OK;
+}
+
+int fpsgpu_server_submit(void* server, const float* points, size_t n_points, size_t dim,
+                         size_t n_samples, size_t start_idx, size_t height,
+                         size_t* sampled_point_indices, uint64_t* ticket) {
+    fpsgpu::clear_error();
+    auto* s = static_cast<Server*>(server);
+    if (!s || !points || !sampled_point_indices || !ticket)
+        return fpsgpu::set_error(FPSGPU_ERR_ARG, "null argument");
+    if (dim == 0 || dim > 8) return fpsgpu::set_error(FPSGPU_ERR_DIM, "dim must be in [1, 8]");
+    if (start_idx >= n_points) return fpsgpu::set_error(FPSGPU_ERR_START, "start_idx out of range");
+    if (n_samples == 0 || height == 0)
+        return fpsgpu::set_error(FPSGPU_ERR_ARG, "n_samples and height must be >= 1");
+    auto r = std::make_unique<Request>();
+    r->pts = points;
+    r->n = n_points;
+    r->dim = dim;
+    r->k = n_samples;
+    r->start = start_idx;
+    r->height = height;
+    r->out = reinterpret_cast<uint64_t*>(sampled_point_indices);
+    r->bytes = fpsgpu::request_bytes(n_points, dim, n_samples);
+    r->t_submit = fpsgpu::now_ms();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        r->id = s->next_id++;
+        *ticket = r->id;
+        s->pending[n_points > fpsgpu::kSmallPoints ? 1 : 0].push_back(r.get());
+        s->reqs.emplace(r->id, std::move(r));
+    }
+    s->cv_work.notify_all();
+    return FPSGPU_OK;
+}
+
+int fpsgpu_server_wait(void* server, uint64_t ticket, double* queue_ms, double* total_ms) {
+    auto* s = static_cast<Server*>(server);
+    if (!s) return fpsgpu::set_error(FPSGPU_ERR_ARG, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return fpsgpu::set_error(FPSGPU_ERR_ARG, "unknown ticket");
+    Request* r = it->second.get();
+    s->cv_done.wait(lk, [&] { return r->done; });
+    const int rc = r->rc;
+    if (queue_ms) *queue_ms = r->t_admit - r->t_submit;
+    if (total_ms) *total_ms = r->t_done - r->t_submit;
+    s->reqs.erase(it);
+    if (rc) return fpsgpu::set_error(rc, "request %llu failed", (unsigned long long)ticket);
+    return FPSGPU_OK;
+}
+
+int fpsgpu_server_destroy(void* server) {
+    auto* s = static_cast<Server*>(server);
+    if (!s) return FPSGPU_OK;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stopping = true;
+    }
+    s->cv_work.notify_all();
+    s->cv_done.notify_all();
+    for (auto& t : s->workers) t.join();
+    delete s;
+    return FPSGPU_OK;
+}
+
+}  // extern "C"

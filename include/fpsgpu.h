@@ -120,6 +120,29 @@ int fpsgpu_kdline_batch_device(const float *d_points, const size_t *h_offsets,
                                uint64_t *d_out, void *stream);
 
 /*
+ * Request server (no counterpart in the reference): bucket_fps_kdline as a
+ * service with continuous batching.  Worker threads, one CUDA stream each,
+ * repeatedly take every waiting request of their size class (at most 262144
+ * points: "small" workers; larger: "large" workers) that fits in the
+ * device-memory budget and run them as one batch; requests arriving meanwhile
+ * go to the next free worker, so batches overlap on the GPU.  Every result is
+ * identical to one bucket_fps_kdline call on that cloud.
+ *   create : budget in bytes of device memory for admitted requests
+ *   submit : host buffers; `points` and `sampled_point_indices` must stay valid
+ *            until fpsgpu_server_wait returns for the ticket
+ *   wait   : blocks until the request is done; queue_ms = time until its
+ *            batch started, total_ms = submit-to-result latency (either may be NULL)
+ *   destroy: finishes the requests already submitted, then stops the workers
+ */
+int fpsgpu_server_create(size_t max_device_bytes, int small_workers, int large_workers,
+                         void **server);
+int fpsgpu_server_submit(void *server, const float *points, size_t n_points, size_t dim,
+                         size_t n_samples, size_t start_idx, size_t height,
+                         size_t *sampled_point_indices, uint64_t *ticket);
+int fpsgpu_server_wait(void *server, uint64_t ticket, double *queue_ms, double *total_ms);
+int fpsgpu_server_destroy(void *server);
+
+/*
  * The kd-line tree build alone (KDTreeBase.h:84-207 of the reference), for
  * inspection and tests: h_perm (n_points, HOST) receives the original index of
  * the point at every position of the permuted order, h_bucket_start (HOST,
