@@ -702,26 +702,26 @@ __device__ __forceinline__ uint64_t recompute_piece(const float* xb, uint64_t xs
 
 // ---- batched sampling: one CTA per cloud -------------------------------------
 //
-// A persistent grid pulls clouds from a queue (largest first).  The cloud's
-// pieces live in shared memory (box, max key, coordinates of the max, start);
-// consecutive runs of 32 pieces -- neighbours in the kd refinement, so close in
-// space -- form groups whose union box and max key are held in registers, one
-// group per lane: group g belongs to warp g % nwarps.  Clouds of at most
-// `mcap` points also keep their points (coordinates, running distance, tag) in
-// shared memory; larger ones read them from L2/HBM.
-// One sample:
-//   1. each warp offers its best group key and that group's max coordinates in
-//      a parity-double-buffered shared array; one __syncthreads; every warp
-//      reduces the offers itself and takes the winner as the reference point r;
-//   2. every lane tests its group box against r; for each dirty group the warp
-//      tests the group's 32 piece boxes (one per lane), recomputes the dirty
-//      pieces (recompute_piece) and refreshes the group max.
-// A sample touches O(groups + dirty groups x 32 + dirty pieces x 128) data
-// instead of testing every piece.  kd-line outputs hold tags while sampling and
-// are mapped to original indices by the CTA after the cloud's last sample.
-constexpr int kBatchThreads = 512;
-constexpr uint32_t kGroup = 32;                  // pieces per group
-constexpr uint32_t kBatchMaxPieces = kGroup * kBatchThreads;  // one group per thread
+// A persistent grid pulls clouds from a queue (largest first).  Every thread
+// owns up to batch_slots(D) pieces of the current cloud and keeps their boxes and
+// max keys in registers; piece q belongs to warp q % nwarps, so pieces that
+// are neighbours in storage order (and tend to turn dirty together) land in
+// different warps.  Clouds of at most `mcap` points keep their points
+// (coordinates, running distance, tag) in shared memory, larger ones read them
+// from L2/HBM.  One sample:
+//   1. every thread tests its pieces against the reference point r (registers
+//      only); a warp recomputes its dirty pieces one after the other
+//      (recompute_piece: one round trip each);
+//   2. each warp offers its best key and that piece's max coordinates in a
+//      parity-double-buffered shared array; one __syncthreads;
+//   3. every warp reduces the 32 offers itself and takes the winner's
+//      coordinates as the next r -- no second barrier, no global load.
+// kd-line outputs hold tags while sampling and are mapped to original indices
+// by the CTA after the cloud's last sample.
+// threads per cloud and pieces per thread: 2048 pieces per cloud either way;
+// 512 threads x 4 slots for D >= 3 keeps the registers from spilling
+constexpr int batch_threads(int D) { return D <= 2 ? 1024 : 512; }
+constexpr int batch_slots(int D) { return 2048 / batch_threads(D); }
 
 struct BatchArgs {
     const float* X;             // SoA [D][n], storage order (all clouds)
@@ -743,29 +743,26 @@ struct BatchArgs {
     uint64_t* out;
     unsigned int* queue;
     unsigned long long* counters;
-    uint32_t cap;               // pieces per cloud at most (shared-memory records)
+    uint32_t cap;               // pieces per cloud at most (batch_slots(D) x threads)
     uint32_t mcap;              // points that fit in shared memory
 };
 
 inline size_t batch_smem_bytes(int D, uint32_t cap, uint32_t mcap) {
-    return (size_t)cap * (8 + 12 * D) + (size_t)(cap + 1) * 4 + (size_t)mcap * (4 * D + 8) + 16;
+    return (size_t)(cap + 1) * 4 + (size_t)cap * D * 4 + (size_t)mcap * (4 * D + 8) + 16;
 }
 
 template <int D, bool FMA, bool KD>
-__global__ void __launch_bounds__(kBatchThreads, 1) batch_sample(BatchArgs a) {
+__global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     __shared__ uint64_t s_wkey[2][32];
     __shared__ float s_wc[2][32][kMaxDim];
     __shared__ uint32_t s_item;
     const uint32_t cap = a.cap, mcap = a.mcap;
-    uint64_t* s_pkey = reinterpret_cast<uint64_t*>(s_dyn);        // [cap]
-    float* s_plo = reinterpret_cast<float*>(s_pkey + cap);         // [D][cap]
-    float* s_phi = s_plo + (size_t)D * cap;                        // [D][cap]
-    float* s_pmc = s_phi + (size_t)D * cap;                        // [D][cap] max coordinates
-    float* s_x = s_pmc + (size_t)D * cap;                          // [D][mcap]
-    float* s_dis = s_x + (size_t)D * mcap;                         // [mcap]
-    uint32_t* s_tag = reinterpret_cast<uint32_t*>(s_dis + mcap);   // [mcap]
-    uint32_t* s_ps = s_tag + mcap;                                 // [cap + 1] local piece starts
+    float* s_x = reinterpret_cast<float*>(s_dyn);                 // [D][mcap]
+    float* s_dis = s_x + (size_t)D * mcap;                        // [mcap]
+    uint32_t* s_tag = reinterpret_cast<uint32_t*>(s_dis + mcap);  // [mcap]
+    uint32_t* s_ps = s_tag + mcap;                                // [cap + 1] local piece starts
+    float* s_mc = reinterpret_cast<float*>(s_ps + cap + 1);       // [D][cap] max coordinates
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const uint32_t T = blockDim.x;
     const uint64_t n = a.n;
@@ -779,23 +776,28 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batch_sample(BatchArgs a) {
         const uint32_t c = a.order[item];
         const uint32_t P0 = a.cloud_piece[c];
         const uint32_t np = a.cloud_piece[c + 1] - P0;
-        const uint32_t ng = (np + kGroup - 1) / kGroup;
         const uint64_t K = a.cloud_k[c];
         const uint64_t coff = a.cloud_off[c];
         const uint32_t nc = (uint32_t)(a.cloud_off[c + 1] - coff);
         const uint64_t ooff = a.out_off[c];
         const bool resident = nc <= mcap;
 
-        for (uint32_t i = tid; i <= np; i += T) {
-            s_ps[i] = a.pstart[P0 + i] - (uint32_t)coff;
-            if (i < np) {
+        // my pieces: slot j holds piece j * T + lane * nwarps + warp
+        float lo[batch_slots(D)][D], hi[batch_slots(D)][D];
+        uint64_t key[batch_slots(D)];
+        uint32_t myq[batch_slots(D)];
 #pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    s_plo[(size_t)d * cap + i] = a.plo[(uint64_t)(P0 + i) * D + d];
-                    s_phi[(size_t)d * cap + i] = a.phi[(uint64_t)(P0 + i) * D + d];
-                }
+        for (int j = 0; j < batch_slots(D); ++j) {
+            myq[j] = (uint32_t)j * T + (uint32_t)lane * nwarps + warp;
+            key[j] = 0;
+            const bool have = myq[j] < np;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                lo[j][d] = have ? a.plo[(uint64_t)(P0 + myq[j]) * D + d] : 0.0f;
+                hi[j][d] = have ? a.phi[(uint64_t)(P0 + myq[j]) * D + d] : 0.0f;
             }
         }
+        for (uint32_t i = tid; i <= np; i += T) s_ps[i] = a.pstart[P0 + i] - (uint32_t)coff;
         if (resident) {
             for (uint32_t i = tid; i < nc; i += T) {
 #pragma unroll
@@ -815,125 +817,57 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batch_sample(BatchArgs a) {
         if (tid == 0 && K > 0) a.out[ooff] = KD ? tag0 : tag0 - coff;
         __syncthreads();
 
-        // first reference point: every piece, warp w taking pieces w, w + nwarps, ...
-        if (K > 1) {
-            for (uint32_t q = warp; q < np; q += nwarps) {
-                const uint32_t ps = s_ps[q], pe = s_ps[q + 1];
-                if (lane == 0) touched += pe - ps;
-                float pc[D];
-                const uint64_t wk = recompute_piece<D, FMA, KD>(xb, xs, disb, tagb, ps, pe, r, true, pc);
-                if (lane == 0) {
-                    s_pkey[q] = wk;
-#pragma unroll
-                    for (int d = 0; d < D; ++d) s_pmc[(size_t)d * cap + q] = pc[d];
-                }
-            }
-        }
-        __syncthreads();
-
-        // my group: g = lane * nwarps + warp; union box and max from its pieces
-        const uint32_t myg = (uint32_t)lane * nwarps + warp;
-        const bool haveg = myg < ng;
-        float glo[D], ghi[D];
-        uint64_t gkey = 0;
-        uint32_t gq = 0;
-        for (uint32_t l = 0; l < 32; ++l) {
-            const uint32_t g = l * nwarps + warp;
-            if (g >= ng) break;  // warp-uniform
-            const uint32_t q = g * kGroup + lane;
-            const bool hp = q < np;
-            float lo[D], hi[D];
-            uint64_t pk = hp ? s_pkey[q] : 0ull;
-#pragma unroll
-            for (int d = 0; d < D; ++d) {
-                lo[d] = hp ? s_plo[(size_t)d * cap + q] : FLT_MAX;
-                hi[d] = hp ? s_phi[(size_t)d * cap + q] : -FLT_MAX;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    lo[d] = fminf(lo[d], __shfl_xor_sync(kFull, lo[d], o));
-                    hi[d] = fmaxf(hi[d], __shfl_xor_sync(kFull, hi[d], o));
-                }
-            }
-            const uint64_t wk = warp_max_key(pk);
-            const int wl = __ffs(__ballot_sync(kFull, hp && pk == wk)) - 1;
-            if (lane == (int)l) {
-#pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    glo[d] = lo[d];
-                    ghi[d] = hi[d];
-                }
-                gkey = wk;
-                gq = g * kGroup + (uint32_t)wl;
-            }
-        }
-
         int par = 0;
         for (uint64_t t = 0; t + 1 < K; ++t) {
-            // 1. offers and the winner
-            {
-                const uint64_t wb = warp_max_key(haveg ? gkey : 0ull);
-                const int owner = __ffs(__ballot_sync(kFull, haveg && gkey == wb)) - 1;
-                const uint32_t qw = __shfl_sync(kFull, gq, owner < 0 ? 0 : owner);
-                if (lane < D) s_wc[par][warp][lane] = wb ? s_pmc[(size_t)lane * cap + qw] : 0.0f;
-                if (lane == 0) s_wkey[par][warp] = wb;
-                __syncthreads();
-                const uint64_t kw = lane < nwarps ? s_wkey[par][lane] : 0ull;
-                const uint64_t g = warp_max_key(kw);
-                const int w = __ffs(__ballot_sync(kFull, lane < nwarps && kw == g)) - 1;
+            uint64_t best = 0;
+            uint32_t bestq = 0;
 #pragma unroll
-                for (int d = 0; d < D; ++d) r[d] = s_wc[par][w][d];
-                if (tid == 0) {
-                    const uint32_t tg = key_pos<KD>(g);
-                    a.out[ooff + t + 1] = KD ? tg : tg - coff;
+            for (int j = 0; j < batch_slots(D); ++j) {
+                const bool have = myq[j] < np;
+                bool dirty = have;
+                if (t > 0) {
+                    tested += have ? 1u : 0u;
+                    dirty = have && box_bound<D, FMA>(lo[j], hi[j], r) < key_dist(key[j]);
                 }
-                par ^= 1;
-            }
-            if (t + 2 >= K) break;  // the last sample needs no update
-            // 2. apply r: group tests, then the pieces of dirty groups
-            if (haveg) ++tested;
-            const bool dg = haveg && box_bound<D, FMA>(glo, ghi, r) < key_dist(gkey);
-            uint32_t m = __ballot_sync(kFull, dg);
-            while (m) {
-                const int l = __ffs(m) - 1;
-                m &= m - 1;
-                const uint32_t g = (uint32_t)l * nwarps + warp;
-                const uint32_t q = g * kGroup + lane;
-                const bool hp = q < np;
-                uint64_t pk = hp ? s_pkey[q] : 0ull;
-                bool dp = false;
-                if (hp) {
-                    ++tested;
-                    float lo[D], hi[D];
-#pragma unroll
-                    for (int d = 0; d < D; ++d) {
-                        lo[d] = s_plo[(size_t)d * cap + q];
-                        hi[d] = s_phi[(size_t)d * cap + q];
-                    }
-                    dp = box_bound<D, FMA>(lo, hi, r) < key_dist(pk);
-                }
-                uint32_t m2 = __ballot_sync(kFull, dp);
-                while (m2) {
-                    const int l2 = __ffs(m2) - 1;
-                    m2 &= m2 - 1;
-                    const uint32_t qq = g * kGroup + (uint32_t)l2;
-                    const uint32_t ps = s_ps[qq], pe = s_ps[qq + 1];
+                uint32_t m = __ballot_sync(kFull, dirty);
+                while (m) {
+                    const int l = __ffs(m) - 1;
+                    m &= m - 1;
+                    const uint32_t q = __shfl_sync(kFull, myq[j], l);
+                    const uint32_t ps = s_ps[q], pe = s_ps[q + 1];
                     if (lane == 0) touched += pe - ps;
                     float pc[D];
-                    const uint64_t wk = recompute_piece<D, FMA, KD>(xb, xs, disb, tagb, ps, pe, r, false, pc);
-                    if (lane == l2) {
-                        pk = wk;
-                        s_pkey[qq] = wk;
+                    const uint64_t wk =
+                        recompute_piece<D, FMA, KD>(xb, xs, disb, tagb, ps, pe, r, t == 0, pc);
+                    if (lane == l) {
+                        key[j] = wk;
 #pragma unroll
-                        for (int d = 0; d < D; ++d) s_pmc[(size_t)d * cap + qq] = pc[d];
+                        for (int d = 0; d < D; ++d) s_mc[(size_t)d * cap + q] = pc[d];
                     }
                 }
-                const uint64_t gk = warp_max_key(pk);
-                const int gl = __ffs(__ballot_sync(kFull, hp && pk == gk)) - 1;
-                if (lane == l) {
-                    gkey = gk;
-                    gq = g * kGroup + (uint32_t)gl;
+                if (have && key[j] > best) {
+                    best = key[j];
+                    bestq = myq[j];
                 }
             }
+            // the warp's offer: best key and its piece's max coordinates
+            const uint64_t wb = warp_max_key(best);
+            const int owner = __ffs(__ballot_sync(kFull, best == wb)) - 1;
+            const uint32_t qw = __shfl_sync(kFull, bestq, owner);
+            if (lane < D) s_wc[par][warp][lane] = wb ? s_mc[(size_t)lane * cap + qw] : 0.0f;
+            if (lane == 0) s_wkey[par][warp] = wb;
+            __syncthreads();
+            // every warp picks the winner itself
+            const uint64_t kw = lane < nwarps ? s_wkey[par][lane] : 0ull;
+            const uint64_t g = warp_max_key(kw);
+            const int w = __ffs(__ballot_sync(kFull, lane < nwarps && kw == g)) - 1;
+#pragma unroll
+            for (int d = 0; d < D; ++d) r[d] = s_wc[par][w][d];
+            if (tid == 0) {
+                const uint32_t tg = key_pos<KD>(g);
+                a.out[ooff + t + 1] = KD ? tg : tg - coff;
+            }
+            par ^= 1;
         }
         __syncthreads();  // thread 0's output writes are visible to the CTA
         if (KD) {
@@ -1644,9 +1578,7 @@ int run_batch(const BatchCall& bc) {
         static_smem = fa.sharedSizeBytes;
     }
     const size_t avail = (size_t)smem_optin - static_smem - 256;
-    // piece records take (8 + 12D + 4) bytes each in shared memory; keep at
-    // least half of it for resident points
-    const uint32_t cap_max = (uint32_t)std::min<size_t>(kBatchMaxPieces, avail / 2 / (8 + 12 * D + 4));
+    const uint32_t cap_max = (uint32_t)batch_slots(D) * batch_threads(D);
     std::vector<uint64_t> out_off(C), tag0(C);
     std::vector<uint32_t> small, big;
     uint64_t acc = 0;
@@ -1724,12 +1656,12 @@ int run_batch(const BatchCall& bc) {
         FPSGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem));
         int per_sm = 0;
-        FPSGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBatchThreads, smem));
+        FPSGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, batch_threads(D), smem));
         const int G = (int)std::min<uint64_t>(small.size(), (uint64_t)std::max(1, per_sm) * bc.sms);
         void* args[] = {&a};
         SamplerTimer timer;
         timer.begin(bc.stream);
-        if ((rc = launch_persistent(kern, G, kBatchThreads, args, smem, bc.stream, false))) return rc;
+        if ((rc = launch_persistent(kern, G, batch_threads(D), args, smem, bc.stream, false))) return rc;
         timer.end(bc.stream);
         unsigned long long h_cnt[2] = {0, 0};
         FPSGPU_CUDA_TRY(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, bc.stream));
