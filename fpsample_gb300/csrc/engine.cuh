@@ -630,15 +630,17 @@ __global__ void __launch_bounds__(kSampleThreads, 1) fps_sample(SampleArgs a) {
 
 // Recomputes one dirty piece [ps, pe) against reference point r: running
 // distances lowered with the reference's strict "<" rule (or initialised to
-// min(init, d) on the first pass), the piece's new max key and the coordinates
-// of its max point (broadcast to the whole warp).  xb/disb/tagb may point to
+// min(init, d) on the first pass) and the piece's new max key (returned to the
+// whole warp).  The one lane holding the max point (keys are unique) writes its
+// coordinates to c_base[d * c_stride]; no shuffles.  xb/disb/tagb may point to
 // shared or global memory; xs is the coordinate stride.  Pieces of at most
 // kPiece points take an unrolled path that issues every load of the piece
 // before the first use, so a piece in global memory costs one round trip.
 template <int D, bool FMA, bool KD>
 __device__ __forceinline__ uint64_t recompute_piece(const float* xb, uint64_t xs, float* disb,
                                                     const uint32_t* tagb, uint32_t ps, uint32_t pe,
-                                                    const float* r, bool first, float* c_out) {
+                                                    const float* r, bool first, float* c_base,
+                                                    uint32_t c_stride) {
     const int lane = threadIdx.x & 31;
     const float init = KD ? FLT_MAX : INFINITY;
     uint64_t pk = 0;
@@ -694,81 +696,11 @@ __device__ __forceinline__ uint64_t recompute_piece(const float* xb, uint64_t xs
         }
     }
     const uint64_t wk = warp_max_key(pk);
-    const int owner = __ffs(__ballot_sync(kFull, pk == wk)) - 1;
+    if (pk == wk && wk != 0) {
 #pragma unroll
-    for (int d = 0; d < D; ++d) c_out[d] = __shfl_sync(kFull, pc[d], owner);
+        for (int d = 0; d < D; ++d) c_base[(size_t)d * c_stride] = pc[d];
+    }
     return wk;
-}
-
-// Recomputes NP (1 or 2) dirty pieces at once, all of at most kPiece points,
-// issuing every load of both before the first use.  Returns the new max keys
-// (warp-uniform); the lane that holds a piece's max point writes that point's
-// coordinates to mc[d * mcs + q] itself, so no shuffles are needed.
-template <int D, bool FMA, bool KD, int NP>
-__device__ __forceinline__ void recompute_small(const float* xb, uint64_t xs, float* disb,
-                                                const uint32_t* tagb, uint32_t ps0, uint32_t pe0,
-                                                uint32_t q0, uint32_t ps1, uint32_t pe1,
-                                                uint32_t q1, const float* r, bool first,
-                                                float* mc, uint32_t mcs, uint64_t& wk0,
-                                                uint64_t& wk1) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t ps[2] = {ps0, ps1}, pe[2] = {pe0, pe1}, q[2] = {q0, q1};
-    uint64_t wk[2];
-    const float init = KD ? FLT_MAX : INFINITY;
-    constexpr int PPL = kPiece / 32;
-    float x[NP][PPL][D], dv[NP][PPL];
-    uint32_t tg[NP][PPL];
-#pragma unroll
-    for (int k = 0; k < NP; ++k) {
-#pragma unroll
-        for (int j = 0; j < PPL; ++j) {
-            const uint32_t p = ps[k] + lane + 32 * j;
-            if (p < pe[k]) {
-#pragma unroll
-                for (int d = 0; d < D; ++d) x[k][j][d] = xb[(uint64_t)d * xs + p];
-                dv[k][j] = first ? init : disb[p];
-                tg[k][j] = tagb[p];
-            }
-        }
-    }
-    uint64_t pk[NP];
-    int bj[NP];
-#pragma unroll
-    for (int k = 0; k < NP; ++k) {
-        pk[k] = 0;
-        bj[k] = 0;
-#pragma unroll
-        for (int j = 0; j < PPL; ++j) {
-            const uint32_t p = ps[k] + lane + 32 * j;
-            if (p < pe[k]) {
-                const float dd = sqdist<D, FMA>(x[k][j], r);
-                float v = dv[k][j];
-                if (dd < v) v = dd;
-                if (first || dd < dv[k][j]) disb[p] = v;
-                const uint64_t kk = make_key<KD>(v, tg[k][j]);
-                if (kk > pk[k]) {
-                    pk[k] = kk;
-                    bj[k] = j;
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < NP; ++k) wk[k] = warp_max_key(pk[k]);
-#pragma unroll
-    for (int k = 0; k < NP; ++k) {
-        const bool mine = pk[k] == wk[k] && wk[k] != 0;
-        if (mine) {  // exactly one lane: keys are unique
-#pragma unroll
-            for (int j = 0; j < PPL; ++j)
-                if (j == bj[k]) {
-#pragma unroll
-                    for (int d = 0; d < D; ++d) mc[(size_t)d * mcs + q[k]] = x[k][j][d];
-                }
-        }
-    }
-    wk0 = wk[0];
-    wk1 = NP > 1 ? wk[1] : 0ull;
 }
 
 // ---- batched sampling: one CTA per cloud -------------------------------------
@@ -892,42 +824,27 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
         for (uint64_t t = 0; t + 1 < K; ++t) {
             uint64_t best = 0;
             uint32_t bestq = 0;
-            bool dirty[batch_slots(D)];
-#pragma unroll
-            for (int j = 0; j < batch_slots(D); ++j) {  // all box tests first (independent)
-                const bool have = myq[j] < np;
-                dirty[j] = have;
-                if (t > 0) {
-                    tested += have ? 1u : 0u;
-                    dirty[j] = have && box_bound<D, FMA>(lo[j], hi[j], r) < key_dist(key[j]);
-                }
-            }
 #pragma unroll
             for (int j = 0; j < batch_slots(D); ++j) {
-                uint32_t m = __ballot_sync(kFull, dirty[j]);
-                while (m) {
-                    const int l0 = __ffs(m) - 1;
-                    m &= m - 1;
-                    const uint32_t q0 = __shfl_sync(kFull, myq[j], l0);
-                    const uint32_t ps0 = s_ps[q0], pe0 = s_ps[q0 + 1];
-                    if (lane == 0) touched += pe0 - ps0;
-                    if (pe0 - ps0 <= kPiece) {
-                        uint64_t wk0, wk1;
-                        recompute_small<D, FMA, KD, 1>(xb, xs, disb, tagb, ps0, pe0, q0, 0, 0, 0,
-                                                       r, t == 0, s_mc, cap, wk0, wk1);
-                        if (lane == l0) key[j] = wk0;
-                    } else {
-                        float pc[D];
-                        const uint64_t wk = recompute_piece<D, FMA, KD>(xb, xs, disb, tagb, ps0,
-                                                                        pe0, r, t == 0, pc);
-                        if (lane == l0) {
-                            key[j] = wk;
-#pragma unroll
-                            for (int d = 0; d < D; ++d) s_mc[(size_t)d * cap + q0] = pc[d];
-                        }
-                    }
+                const bool have = myq[j] < np;
+                bool dirty = have;
+                if (t > 0) {
+                    tested += have ? 1u : 0u;
+                    dirty = have && box_bound<D, FMA>(lo[j], hi[j], r) < key_dist(key[j]);
                 }
-                if (myq[j] < np && key[j] > best) {
+                uint32_t m = __ballot_sync(kFull, dirty);
+                while (m) {
+                    const int l = __ffs(m) - 1;
+                    m &= m - 1;
+                    const uint32_t q = __shfl_sync(kFull, myq[j], l);
+                    const uint32_t ps = s_ps[q], pe = s_ps[q + 1];
+                    if (lane == 0) touched += pe - ps;
+                    const uint64_t wk =
+                        recompute_piece<D, FMA, KD>(xb, xs, disb, tagb, ps, pe, r, t == 0,
+                                                    s_mc + q, cap);
+                    if (lane == l) key[j] = wk;
+                }
+                if (have && key[j] > best) {
                     best = key[j];
                     bestq = myq[j];
                 }
