@@ -123,6 +123,18 @@ def test_more_samples_than_points_c_abi(mode):
     np.testing.assert_array_equal(capi.fps(pts, 100, 3), ORACLE.fps(pts, 100, 3, mode))
 
 
+@pytest.mark.parametrize("n", [9000, 60_000, 240_000, 400_000])
+def test_single_call_both_sides_of_the_one_cta_limit(n, mode):
+    # single calls whose pieces fit one CTA run on one CTA, larger clouds on
+    # the multi-CTA sampler; kd-line and single-start vanilla on both sides
+    rng = np.random.default_rng(n)
+    pts = rng.random((n, 3), dtype=np.float32)
+    k = 1500
+    np.testing.assert_array_equal(fps.bucket_fps_kdline_sampling(pts, k, 7, n // 3),
+                                  ORACLE.kdline(pts, k, 7, n // 3, mode))
+    np.testing.assert_array_equal(fps.fps_sampling(pts, k, n // 5), ORACLE.fps(pts, k, n // 5, mode))
+
+
 def test_high_dimension_vanilla(mode):
     rng = np.random.default_rng(5)
     for d in (9, 16, 33):
