@@ -636,11 +636,29 @@ __global__ void __launch_bounds__(kSampleThreads, 1) fps_sample(SampleArgs a) {
 // shared or global memory; xs is the coordinate stride.  Pieces of at most
 // kPiece points take an unrolled path that issues every load of the piece
 // before the first use, so a piece in global memory costs one round trip.
+// Keys of the batched sampler: valid bit | distance bits | 21-bit cloud-local
+// position (complemented for kd-line, where the lowest position wins ties) |
+// 11-bit piece index.  Positions are unique, so the order is the one of
+// make_key; the piece index rides along to locate the winner's coordinates.
+constexpr uint32_t kBatchPosBits = 21, kBatchPieceBits = 11;
+template <bool KD>
+__device__ __forceinline__ uint64_t batch_key(float dist, uint32_t local, uint32_t q) {
+    const uint32_t m = (1u << kBatchPosBits) - 1;
+    const uint32_t f = KD ? m - local : local;
+    return kKeyValid | ((uint64_t)__float_as_uint(dist) << 32) | (f << kBatchPieceBits) | q;
+}
+template <bool KD>
+__device__ __forceinline__ uint32_t batch_key_pos(uint64_t key) {
+    const uint32_t m = (1u << kBatchPosBits) - 1;
+    const uint32_t f = ((uint32_t)key >> kBatchPieceBits) & m;
+    return KD ? m - f : f;
+}
+
 template <int D, bool FMA, bool KD>
 __device__ __forceinline__ uint64_t recompute_piece(const float* xb, uint64_t xs, float* disb,
                                                     const uint32_t* tagb, uint32_t ps, uint32_t pe,
                                                     const float* r, bool first, float* c_base,
-                                                    uint32_t c_stride) {
+                                                    uint32_t c_stride, uint32_t tag_base, uint32_t q) {
     const int lane = threadIdx.x & 31;
     const float init = KD ? FLT_MAX : INFINITY;
     uint64_t pk = 0;
@@ -669,7 +687,7 @@ __device__ __forceinline__ uint64_t recompute_piece(const float* xb, uint64_t xs
                 float v = dv[j];
                 if (dd < v) v = dd;
                 if (first || dd < dv[j]) disb[p] = v;
-                const uint64_t kk = make_key<KD>(v, tg[j]);
+                const uint64_t kk = batch_key<KD>(v, tg[j] - tag_base, q);
                 if (kk > pk) {
                     pk = kk;
 #pragma unroll
@@ -687,7 +705,7 @@ __device__ __forceinline__ uint64_t recompute_piece(const float* xb, uint64_t xs
             float v = old;
             if (dd < v) v = dd;
             if (first || dd < old) disb[p] = v;
-            const uint64_t kk = make_key<KD>(v, tagb[p]);
+            const uint64_t kk = batch_key<KD>(v, tagb[p] - tag_base, q);
             if (kk > pk) {
                 pk = kk;
 #pragma unroll
@@ -712,19 +730,26 @@ __device__ __forceinline__ uint64_t recompute_piece(const float* xb, uint64_t xs
 // different warps.  Clouds of at most `mcap` points keep their points
 // (coordinates, running distance, tag) in shared memory, larger ones read them
 // from L2/HBM.  One sample:
-//   1. every thread tests its pieces against the reference point r (registers
-//      only); a warp recomputes its dirty pieces one after the other
-//      (recompute_piece: one round trip each);
-//   2. each warp offers its best key and that piece's max coordinates in a
-//      parity-double-buffered shared array; one __syncthreads;
-//   3. every warp reduces the 32 offers itself and takes the winner's
-//      coordinates as the next r -- no second barrier, no global load.
+//   1. every thread tests all its pieces against the reference point r
+//      (registers only; an empty slot holds an inverted box that is never
+//      dirty), then the warp recomputes its dirty pieces one after the other
+//      (recompute_piece: one round trip each; the lane holding a piece's max
+//      point writes its coordinates to shared memory);
+//   2. lane and warp maxima are recomputed only where a key changed; each
+//      warp folds its max into one shared 64-bit atomicMax word (three of
+//      them rotate, so clearing the previous one never races); one
+//      __syncthreads;
+//   3. the max key carries the winner's piece index (batch_key), so every warp
+//      reads the next r from that piece's max coordinates: two shared loads.
 // kd-line outputs hold tags while sampling and are mapped to original indices
 // by the CTA after the cloud's last sample.
 // threads per cloud and pieces per thread: 2048 pieces per cloud either way;
 // 512 threads x 4 slots for D >= 3 keeps the registers from spilling
 constexpr int batch_threads(int D) { return D <= 2 ? 1024 : 512; }
 constexpr int batch_slots(int D) { return 2048 / batch_threads(D); }
+// batch_key packs a piece index below 2048 and a position below 2^21
+static_assert(2048 <= (1u << kBatchPieceBits), "piece index must fit batch_key");
+static_assert(2048ull * kPiece <= (1ull << kBatchPosBits), "cloud positions must fit batch_key");
 
 struct BatchArgs {
     const float* X;             // SoA [D][n], storage order (all clouds)
@@ -757,8 +782,7 @@ inline size_t batch_smem_bytes(int D, uint32_t cap, uint32_t mcap) {
 template <int D, bool FMA, bool KD>
 __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
-    __shared__ uint64_t s_wkey[2][32];
-    __shared__ float s_wc[2][32][kMaxDim];
+    __shared__ unsigned long long s_best[3];  // rotating per-sample max key
     __shared__ uint32_t s_item;
     const uint32_t cap = a.cap, mcap = a.mcap;
     float* s_x = reinterpret_cast<float*>(s_dyn);                 // [D][mcap]
@@ -794,10 +818,11 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
             myq[j] = (uint32_t)j * T + (uint32_t)lane * nwarps + warp;
             key[j] = 0;
             const bool have = myq[j] < np;
+            // an empty slot gets an inverted box: never nearer than its key 0
 #pragma unroll
             for (int d = 0; d < D; ++d) {
-                lo[j][d] = have ? a.plo[(uint64_t)(P0 + myq[j]) * D + d] : 0.0f;
-                hi[j][d] = have ? a.phi[(uint64_t)(P0 + myq[j]) * D + d] : 0.0f;
+                lo[j][d] = have ? a.plo[(uint64_t)(P0 + myq[j]) * D + d] : INFINITY;
+                hi[j][d] = have ? a.phi[(uint64_t)(P0 + myq[j]) * D + d] : -INFINITY;
             }
         }
         for (uint32_t i = tid; i <= np; i += T) s_ps[i] = a.pstart[P0 + i] - (uint32_t)coff;
@@ -818,55 +843,66 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
         for (int d = 0; d < D; ++d) r[d] = a.Xref[(uint64_t)d * n + tag0];
         // outputs hold tags while sampling (kd-line tags are mapped at the end)
         if (tid == 0 && K > 0) a.out[ooff] = KD ? tag0 : tag0 - coff;
+        if (tid < 3) s_best[tid] = 0ull;
         __syncthreads();
 
-        int par = 0;
+        {
+            // every held piece is tested once per sample after the second
+            uint32_t mine = 0;
+#pragma unroll
+            for (int j = 0; j < batch_slots(D); ++j) mine += myq[j] < np ? 1u : 0u;
+            if (K > 2) tested += (unsigned long long)mine * (K - 2);
+        }
+        int par = 0;  // s_best slot of this sample, rotating over three
+        uint64_t lbest = 0, wbest = 0;  // my best key; the warp's (warp-uniform)
         for (uint64_t t = 0; t + 1 < K; ++t) {
-            uint64_t best = 0;
-            uint32_t bestq = 0;
+            const bool first = t == 0;
+            uint32_t dm = 0;  // my dirty slots, one bit each
 #pragma unroll
             for (int j = 0; j < batch_slots(D); ++j) {
-                const bool have = myq[j] < np;
-                bool dirty = have;
-                if (t > 0) {
-                    tested += have ? 1u : 0u;
-                    dirty = have && box_bound<D, FMA>(lo[j], hi[j], r) < key_dist(key[j]);
-                }
-                uint32_t m = __ballot_sync(kFull, dirty);
-                while (m) {
-                    const int l = __ffs(m) - 1;
-                    m &= m - 1;
-                    const uint32_t q = __shfl_sync(kFull, myq[j], l);
-                    const uint32_t ps = s_ps[q], pe = s_ps[q + 1];
-                    if (lane == 0) touched += pe - ps;
-                    const uint64_t wk =
-                        recompute_piece<D, FMA, KD>(xb, xs, disb, tagb, ps, pe, r, t == 0,
-                                                    s_mc + q, cap);
-                    if (lane == l) key[j] = wk;
-                }
-                if (have && key[j] > best) {
-                    best = key[j];
-                    bestq = myq[j];
-                }
+                const bool dj = first ? myq[j] < np
+                                      : box_bound<D, FMA>(lo[j], hi[j], r) < key_dist(key[j]);
+                dm |= (uint32_t)dj << j;
             }
-            // the warp's offer: best key and its piece's max coordinates
-            const uint64_t wb = warp_max_key(best);
-            const int owner = __ffs(__ballot_sync(kFull, best == wb)) - 1;
-            const uint32_t qw = __shfl_sync(kFull, bestq, owner);
-            if (lane < D) s_wc[par][warp][lane] = wb ? s_mc[(size_t)lane * cap + qw] : 0.0f;
-            if (lane == 0) s_wkey[par][warp] = wb;
-            __syncthreads();
-            // every warp picks the winner itself
-            const uint64_t kw = lane < nwarps ? s_wkey[par][lane] : 0ull;
-            const uint64_t g = warp_max_key(kw);
-            const int w = __ffs(__ballot_sync(kFull, lane < nwarps && kw == g)) - 1;
+            // keys change only in dirty slots: the lane and warp maxima are
+            // recomputed only where something was dirty
+            if (__any_sync(kFull, dm != 0)) {
 #pragma unroll
-            for (int d = 0; d < D; ++d) r[d] = s_wc[par][w][d];
-            if (tid == 0) {
-                const uint32_t tg = key_pos<KD>(g);
-                a.out[ooff + t + 1] = KD ? tg : tg - coff;
+                for (int j = 0; j < batch_slots(D); ++j) {
+                    uint32_t m = __ballot_sync(kFull, (dm >> j) & 1u);
+                    while (m) {
+                        const int l = __ffs(m) - 1;
+                        m &= m - 1;
+                        const uint32_t q = __shfl_sync(kFull, myq[j], l);
+                        const uint32_t ps = s_ps[q], pe = s_ps[q + 1];
+                        if (lane == 0) touched += pe - ps;
+                        const uint64_t wk =
+                            recompute_piece<D, FMA, KD>(xb, xs, disb, tagb, ps, pe, r, first,
+                                                        s_mc + q, cap, (uint32_t)coff, q);
+                        if (lane == l) key[j] = wk;
+                    }
+                }
+                if (dm) {
+                    lbest = 0;
+#pragma unroll
+                    for (int j = 0; j < batch_slots(D); ++j) lbest = key[j] > lbest ? key[j] : lbest;
+                }
+                wbest = warp_max_key(lbest);
             }
-            par ^= 1;
+            // the warp's best goes into the CTA max; the key names the piece
+            // whose max coordinates become the next reference point
+            if (lane == 0 && wbest) atomicMax(&s_best[par], (unsigned long long)wbest);
+            __syncthreads();
+            const uint64_t g = s_best[par];
+            const uint32_t qw = (uint32_t)g & ((1u << kBatchPieceBits) - 1);
+#pragma unroll
+            for (int d = 0; d < D; ++d) r[d] = s_mc[(size_t)d * cap + qw];
+            if (tid == 0) {
+                const uint32_t loc = batch_key_pos<KD>(g);
+                a.out[ooff + t + 1] = KD ? loc + (uint32_t)coff : loc;
+                s_best[par == 0 ? 2 : par - 1] = 0ull;  // last sample's slot: everyone has read it
+            }
+            par = par == 2 ? 0 : par + 1;
         }
         __syncthreads();  // thread 0's output writes are visible to the CTA
         if (KD) {

@@ -70,9 +70,9 @@ __device__ __forceinline__ float box_bound(const float* lo, const float* hi, con
     float acc = 0.0f;
 #pragma unroll
     for (int j = 0; j < D; ++j) {
-        float g = 0.0f;
-        if (r[j] > hi[j]) g = __fsub_rn(r[j], hi[j]);
-        else if (r[j] < lo[j]) g = __fsub_rn(lo[j], r[j]);
+        // r above the box: r - hi > 0 > lo - r; below: lo - r > 0 > r - hi;
+        // inside: both <= 0.  Same value as the branchy form, fewer steps.
+        const float g = fmaxf(fmaxf(__fsub_rn(lo[j], r[j]), __fsub_rn(r[j], hi[j])), 0.0f);
         if (j == 0) acc = __fmul_rn(g, g);
         else acc = FMA ? __fmaf_rn(g, g, acc) : __fadd_rn(acc, __fmul_rn(g, g));
     }
