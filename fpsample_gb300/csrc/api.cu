@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 #include <string>
@@ -87,6 +88,71 @@ int launch_persistent(const void* func, int grid, int block, void** args, size_t
     } else {
         FPSGPU_CUDA_TRY(cudaLaunchKernel(func, dim3(grid), dim3(block), args, smem, stream));
     }
+    return FPSGPU_OK;
+}
+
+// Cluster size of the batched engine's cluster sampler: FPSGPU_CLUSTER_SIZE
+// (1 turns clusters off; 2, 4, 8 or 16), default 8; clouds that need more CTAs
+// get the next power of two up to 16.
+int cluster_size_for_batch() {
+    static const int v = [] {
+        const char* e = std::getenv("FPSGPU_CLUSTER_SIZE");
+        if (!e) return 8;
+        const int x = std::atoi(e);
+        return (x == 1 || x == 2 || x == 4 || x == 8 || x == 16) ? x : 8;
+    }();
+    return v;
+}
+
+// How many clusters of `cl` CTAs of `func` can be resident at once (0: none).
+int cluster_capacity(const void* func, int cl, int block, size_t smem, int* out) {
+    *out = 0;
+    if (cl > 8)
+        FPSGPU_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    FPSGPU_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)cl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)cl);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveClusters(&n, func, &cfg);
+    if (e != cudaSuccess) {  // e.g. a cluster size the device does not allow
+        cudaGetLastError();
+        return FPSGPU_OK;
+    }
+    *out = n;
+    return FPSGPU_OK;
+}
+
+// Persistent cluster launch: min(items, resident clusters) clusters of `cl`
+// CTAs; the kernel's clusters take items from a queue.
+int launch_clustered(const void* func, int items, int cl, int block, void** args, size_t smem,
+                     cudaStream_t stream) {
+    int maxc = 0;
+    int rc = cluster_capacity(func, cl, block, smem, &maxc);
+    if (rc) return rc;
+    if (maxc < 1) return set_error(FPSGPU_ERR_CUDA, "no cluster of %d CTAs fits on this GPU", cl);
+    stats_count_launch();
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)cl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)(std::min(items, maxc) * cl));
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    FPSGPU_CUDA_TRY(cudaLaunchKernelExC(&cfg, func, args));
     return FPSGPU_OK;
 }
 

@@ -743,6 +743,15 @@ __device__ __forceinline__ uint64_t recompute_piece(const float* xb, uint64_t xs
 //      reads the next r from that piece's max coordinates: two shared loads.
 // kd-line outputs hold tags while sampling and are mapped to original indices
 // by the CTA after the cloud's last sample.
+//
+// CL = true: one thread-block cluster of C CTAs per cloud, for clouds with more
+// pieces than one CTA holds.  Piece q belongs to CTA q % C (neighbouring
+// pieces, which turn dirty together, land in different CTAs) and to its slot
+// q / C there; points stay in L2/HBM.  Step 3 becomes a cluster exchange:
+// warp 0 of every CTA stores its CTA's max key and the coordinates behind it
+// into every CTA's shared memory (DSMEM), one cluster barrier, and every warp
+// reduces the C records locally.  Cluster rank 0 takes the items from the
+// queue and writes the outputs.
 // threads per cloud and pieces per thread: 2048 pieces per cloud either way;
 // 512 threads x 4 slots for D >= 3 keeps the registers from spilling
 constexpr int batch_threads(int D) { return D <= 2 ? 1024 : 512; }
@@ -750,6 +759,11 @@ constexpr int batch_slots(int D) { return 2048 / batch_threads(D); }
 // batch_key packs a piece index below 2048 and a position below 2^21
 static_assert(2048 <= (1u << kBatchPieceBits), "piece index must fit batch_key");
 static_assert(2048ull * kPiece <= (1ull << kBatchPosBits), "cloud positions must fit batch_key");
+
+// batch clouds use cloud-local positions in 21 key bits
+constexpr uint64_t kBatchMaxCloudPoints = 1ull << kBatchPosBits;
+// largest cluster the cluster sampler launches (16 needs the non-portable size)
+constexpr int kMaxCluster = 16;
 
 struct BatchArgs {
     const float* X;             // SoA [D][n], storage order (all clouds)
@@ -776,28 +790,42 @@ struct BatchArgs {
 };
 
 inline size_t batch_smem_bytes(int D, uint32_t cap, uint32_t mcap) {
-    return (size_t)(cap + 1) * 4 + (size_t)cap * D * 4 + (size_t)mcap * (4 * D + 8) + 16;
+    return (size_t)cap * 8 + (size_t)cap * D * 4 + (size_t)mcap * (4 * D + 8) + 16;
 }
 
-template <int D, bool FMA, bool KD>
+template <int D, bool FMA, bool KD, bool CL>
 __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     __shared__ unsigned long long s_best[3];  // rotating per-sample max key
     __shared__ uint32_t s_item;
+    // cluster exchange records, double-buffered by sample parity
+    __shared__ uint64_t s_xkey[2][CL ? kMaxCluster : 1];
+    __shared__ float s_xc[2][CL ? kMaxCluster : 1][D];
     const uint32_t cap = a.cap, mcap = a.mcap;
     float* s_x = reinterpret_cast<float*>(s_dyn);                 // [D][mcap]
     float* s_dis = s_x + (size_t)D * mcap;                        // [mcap]
     uint32_t* s_tag = reinterpret_cast<uint32_t*>(s_dis + mcap);  // [mcap]
-    uint32_t* s_ps = s_tag + mcap;                                // [cap + 1] local piece starts
-    float* s_mc = reinterpret_cast<float*>(s_ps + cap + 1);       // [D][cap] max coordinates
+    uint32_t* s_ps = s_tag + mcap;                                // [cap] my pieces' starts
+    uint32_t* s_pe = s_ps + cap;                                  // [cap] and ends
+    float* s_mc = reinterpret_cast<float*>(s_pe + cap);           // [D][cap] max coordinates
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const uint32_t T = blockDim.x;
+    const uint32_t C = CL ? cluster_size() : 1u, rank = CL ? cluster_rank() : 0u;
     const uint64_t n = a.n;
     unsigned long long tested = 0, touched = 0;
 
     for (;;) {
-        if (tid == 0) s_item = atomicAdd(a.queue, 1u);
-        __syncthreads();
+        if (CL) {
+            // rank 0 takes the item; the others read it from rank 0's shared
+            // memory; the second barrier keeps rank 0 from overwriting it early
+            if (rank == 0 && tid == 0) s_item = atomicAdd(a.queue, 1u);
+            cluster_sync_all();
+            if (rank != 0 && tid == 0) s_item = dsmem_ld_u32(dsmem_addr(&s_item, 0));
+            cluster_sync_all();
+        } else {
+            if (tid == 0) s_item = atomicAdd(a.queue, 1u);
+            __syncthreads();
+        }
         const uint32_t item = s_item;
         if (item >= a.n_items) break;
         const uint32_t c = a.order[item];
@@ -809,7 +837,9 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
         const uint64_t ooff = a.out_off[c];
         const bool resident = nc <= mcap;
 
-        // my pieces: slot j holds piece j * T + lane * nwarps + warp
+        // my pieces: slot j holds local piece j * T + lane * nwarps + warp,
+        // which is the cloud's piece local * C + rank
+        const uint32_t nmine = np > rank ? (np - rank + C - 1) / C : 0u;
         float lo[batch_slots(D)][D], hi[batch_slots(D)][D];
         uint64_t key[batch_slots(D)];
         uint32_t myq[batch_slots(D)];
@@ -817,15 +847,20 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
         for (int j = 0; j < batch_slots(D); ++j) {
             myq[j] = (uint32_t)j * T + (uint32_t)lane * nwarps + warp;
             key[j] = 0;
-            const bool have = myq[j] < np;
+            const bool have = myq[j] < nmine;
+            const uint64_t q = (uint64_t)P0 + (uint64_t)myq[j] * C + rank;
             // an empty slot gets an inverted box: never nearer than its key 0
 #pragma unroll
             for (int d = 0; d < D; ++d) {
-                lo[j][d] = have ? a.plo[(uint64_t)(P0 + myq[j]) * D + d] : INFINITY;
-                hi[j][d] = have ? a.phi[(uint64_t)(P0 + myq[j]) * D + d] : -INFINITY;
+                lo[j][d] = have ? a.plo[q * D + d] : INFINITY;
+                hi[j][d] = have ? a.phi[q * D + d] : -INFINITY;
             }
         }
-        for (uint32_t i = tid; i <= np; i += T) s_ps[i] = a.pstart[P0 + i] - (uint32_t)coff;
+        for (uint32_t i = tid; i < nmine; i += T) {
+            const uint64_t q = (uint64_t)P0 + (uint64_t)i * C + rank;
+            s_ps[i] = a.pstart[q] - (uint32_t)coff;
+            s_pe[i] = a.pstart[q + 1] - (uint32_t)coff;
+        }
         if (resident) {
             for (uint32_t i = tid; i < nc; i += T) {
 #pragma unroll
@@ -842,7 +877,7 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
 #pragma unroll
         for (int d = 0; d < D; ++d) r[d] = a.Xref[(uint64_t)d * n + tag0];
         // outputs hold tags while sampling (kd-line tags are mapped at the end)
-        if (tid == 0 && K > 0) a.out[ooff] = KD ? tag0 : tag0 - coff;
+        if (rank == 0 && tid == 0 && K > 0) a.out[ooff] = KD ? tag0 : tag0 - coff;
         if (tid < 3) s_best[tid] = 0ull;
         __syncthreads();
 
@@ -850,9 +885,10 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
             // every held piece is tested once per sample after the second
             uint32_t mine = 0;
 #pragma unroll
-            for (int j = 0; j < batch_slots(D); ++j) mine += myq[j] < np ? 1u : 0u;
+            for (int j = 0; j < batch_slots(D); ++j) mine += myq[j] < nmine ? 1u : 0u;
             if (K > 2) tested += (unsigned long long)mine * (K - 2);
         }
+        int px = 0;   // cluster record buffer of this sample
         int par = 0;  // s_best slot of this sample, rotating over three
         uint64_t lbest = 0, wbest = 0;  // my best key; the warp's (warp-uniform)
         for (uint64_t t = 0; t + 1 < K; ++t) {
@@ -860,7 +896,7 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
             uint32_t dm = 0;  // my dirty slots, one bit each
 #pragma unroll
             for (int j = 0; j < batch_slots(D); ++j) {
-                const bool dj = first ? myq[j] < np
+                const bool dj = first ? myq[j] < nmine
                                       : box_bound<D, FMA>(lo[j], hi[j], r) < key_dist(key[j]);
                 dm |= (uint32_t)dj << j;
             }
@@ -874,7 +910,7 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
                         const int l = __ffs(m) - 1;
                         m &= m - 1;
                         const uint32_t q = __shfl_sync(kFull, myq[j], l);
-                        const uint32_t ps = s_ps[q], pe = s_ps[q + 1];
+                        const uint32_t ps = s_ps[q], pe = s_pe[q];
                         if (lane == 0) touched += pe - ps;
                         const uint64_t wk =
                             recompute_piece<D, FMA, KD>(xb, xs, disb, tagb, ps, pe, r, first,
@@ -893,19 +929,45 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
             // whose max coordinates become the next reference point
             if (lane == 0 && wbest) atomicMax(&s_best[par], (unsigned long long)wbest);
             __syncthreads();
-            const uint64_t g = s_best[par];
-            const uint32_t qw = (uint32_t)g & ((1u << kBatchPieceBits) - 1);
+            uint64_t g;
+            if (CL) {
+                if (warp == 0) {
+                    // my CTA's record into every CTA of the cluster (a CTA
+                    // without pieces sends key 0, which never wins)
+                    const uint64_t gl = s_best[par];
+                    if ((uint32_t)lane < C) {
+                        const uint32_t qw = (uint32_t)gl & ((1u << kBatchPieceBits) - 1);
+                        dsmem_st_u64(dsmem_addr(&s_xkey[px][rank], lane), gl);
 #pragma unroll
-            for (int d = 0; d < D; ++d) r[d] = s_mc[(size_t)d * cap + qw];
+                        for (int d = 0; d < D; ++d)
+                            dsmem_st_f32(dsmem_addr(&s_xc[px][rank][d], lane),
+                                         gl ? s_mc[(size_t)d * cap + qw] : 0.0f);
+                    }
+                }
+                cluster_sync_all();
+                const uint64_t kx = (uint32_t)lane < C ? s_xkey[px][lane] : 0ull;
+                g = warp_max_key(kx);
+                const int w = __ffs(__ballot_sync(kFull, (uint32_t)lane < C && kx == g)) - 1;
+#pragma unroll
+                for (int d = 0; d < D; ++d) r[d] = s_xc[px][w][d];
+                px ^= 1;
+            } else {
+                g = s_best[par];
+                const uint32_t qw = (uint32_t)g & ((1u << kBatchPieceBits) - 1);
+#pragma unroll
+                for (int d = 0; d < D; ++d) r[d] = s_mc[(size_t)d * cap + qw];
+            }
             if (tid == 0) {
-                const uint32_t loc = batch_key_pos<KD>(g);
-                a.out[ooff + t + 1] = KD ? loc + (uint32_t)coff : loc;
+                if (rank == 0) {
+                    const uint32_t loc = batch_key_pos<KD>(g);
+                    a.out[ooff + t + 1] = KD ? loc + (uint32_t)coff : loc;
+                }
                 s_best[par == 0 ? 2 : par - 1] = 0ull;  // last sample's slot: everyone has read it
             }
             par = par == 2 ? 0 : par + 1;
         }
         __syncthreads();  // thread 0's output writes are visible to the CTA
-        if (KD) {
+        if (KD && rank == 0) {
             for (uint64_t i = tid; i < K; i += T) a.out[ooff + i] = a.idmap[a.out[ooff + i]] - coff;
         }
     }
@@ -1609,15 +1671,16 @@ int run_batch(const BatchCall& bc) {
     size_t static_smem = 0;
     {
         cudaFuncAttributes fa{};
-        FPSGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)batch_sample<D, FMA, true>));
+        FPSGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)batch_sample<D, FMA, true, false>));
         static_smem = fa.sharedSizeBytes;
     }
     const size_t avail = (size_t)smem_optin - static_smem - 256;
     const uint32_t cap_max = (uint32_t)batch_slots(D) * batch_threads(D);
+    const int want_cluster = cluster_size_for_batch();
     std::vector<uint64_t> out_off(C), tag0(C);
-    std::vector<uint32_t> small, big;
+    std::vector<uint32_t> small, clustered, big;
     uint64_t acc = 0;
-    uint32_t cap = 1;
+    uint32_t cap = 1, need_cl = 1;
     for (size_t c = 0; c < C; ++c) {
         out_off[c] = acc;
         acc += bc.k[c];
@@ -1625,20 +1688,40 @@ int run_batch(const BatchCall& bc) {
         // a tag; vanilla: the start is an original index, also a tag
         tag0[c] = bc.off[c] + bc.start[c];
         const uint32_t np = h_cpiece[c + 1] - h_cpiece[c];
+        const uint64_t nc = bc.off[c + 1] - bc.off[c];
         if (bc.k[c] == 0) continue;
         if (np <= cap_max) {
             small.push_back((uint32_t)c);
             cap = std::max(cap, np);
+        } else if (want_cluster > 1 && np <= (uint64_t)kMaxCluster * cap_max &&
+                   nc <= kBatchMaxCloudPoints) {
+            clustered.push_back((uint32_t)c);
+            need_cl = std::max<uint32_t>(need_cl, (np + cap_max - 1) / cap_max);
         } else {
             big.push_back((uint32_t)c);
         }
     }
     // largest first
-    std::sort(small.begin(), small.end(), [&](uint32_t x, uint32_t y) {
+    auto by_work = [&](uint32_t x, uint32_t y) {
         return bc.k[x] * (bc.off[x + 1] - bc.off[x]) > bc.k[y] * (bc.off[y + 1] - bc.off[y]);
-    });
+    };
+    std::sort(small.begin(), small.end(), by_work);
+    std::sort(clustered.begin(), clustered.end(), by_work);
+    int cl = want_cluster;
+    while ((uint32_t)cl < need_cl) cl *= 2;
+    const void* cl_kern = bc.kd ? (const void*)batch_sample<D, FMA, true, true>
+                                : (const void*)batch_sample<D, FMA, false, true>;
+    const size_t cl_smem = batch_smem_bytes(D, cap_max, 0);
+    if (!clustered.empty()) {
+        int maxc = 0;
+        if ((rc = cluster_capacity(cl_kern, cl, batch_threads(D), cl_smem, &maxc))) return rc;
+        if (maxc < 1) {  // no such cluster on this device: the grid sampler takes them
+            big.insert(big.end(), clustered.begin(), clustered.end());
+            clustered.clear();
+        }
+    }
 
-    if (!small.empty()) {
+    if (!small.empty() || !clustered.empty()) {
         uint64_t *d_k, *d_tag0, *d_ooff;
         uint32_t* d_order;
         unsigned int* d_queue;
@@ -1647,16 +1730,18 @@ int run_batch(const BatchCall& bc) {
         if ((rc = sc.alloc(&d_k, C))) return rc;
         if ((rc = sc.alloc(&d_tag0, C))) return rc;
         if ((rc = sc.alloc(&d_ooff, C))) return rc;
-        if ((rc = sc.alloc(&d_order, small.size()))) return rc;
-        if ((rc = sc.alloc(&d_queue, 1))) return rc;
+        if ((rc = sc.alloc(&d_order, small.size() + clustered.size()))) return rc;
+        if ((rc = sc.alloc(&d_queue, 2))) return rc;
         if ((rc = sc.alloc(&cnt, 2))) return rc;
         if ((rc = sc.alloc(&dis, n))) return rc;
         FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_k, bc.k.data(), C * 8, cudaMemcpyHostToDevice, bc.stream));
         FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_tag0, tag0.data(), C * 8, cudaMemcpyHostToDevice, bc.stream));
         FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_ooff, out_off.data(), C * 8, cudaMemcpyHostToDevice, bc.stream));
-        FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_order, small.data(), small.size() * 4,
+        std::vector<uint32_t> order(small);
+        order.insert(order.end(), clustered.begin(), clustered.end());
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_order, order.data(), order.size() * 4,
                                         cudaMemcpyHostToDevice, bc.stream));
-        FPSGPU_CUDA_TRY(cudaMemsetAsync(d_queue, 0, sizeof(unsigned int), bc.stream));
+        FPSGPU_CUDA_TRY(cudaMemsetAsync(d_queue, 0, 2 * sizeof(unsigned int), bc.stream));
         FPSGPU_CUDA_TRY(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), bc.stream));
         BatchArgs a{};
         a.X = bt.X;
@@ -1671,38 +1756,55 @@ int run_batch(const BatchCall& bc) {
         a.cloud_k = d_k;
         a.cloud_tag0 = d_tag0;
         a.out_off = d_ooff;
-        a.order = d_order;
-        a.n_items = (uint32_t)small.size();
         a.Xref = bt.Xref;
         a.idmap = bt.idsnap;
         a.out = bc.d_out;
-        a.queue = d_queue;
         a.counters = cnt;
-        a.cap = cap;
-        // what the piece starts and max coordinates leave of shared memory holds
-        // small clouds' points
-        uint64_t max_nc = 0;
-        for (uint32_t c : small) max_nc = std::max<uint64_t>(max_nc, bc.off[c + 1] - bc.off[c]);
-        const size_t left = avail - batch_smem_bytes(D, cap, 0);
-        a.mcap = (uint32_t)std::min<uint64_t>(left / (4 * D + 8), max_nc);
-        const size_t smem = batch_smem_bytes(D, cap, a.mcap);
-        const void* kern = bc.kd ? (const void*)batch_sample<D, FMA, true>
-                                 : (const void*)batch_sample<D, FMA, false>;
-        FPSGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem));
-        int per_sm = 0;
-        FPSGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, batch_threads(D), smem));
-        const int G = (int)std::min<uint64_t>(small.size(), (uint64_t)std::max(1, per_sm) * bc.sms);
-        void* args[] = {&a};
         SamplerTimer timer;
         timer.begin(bc.stream);
-        if ((rc = launch_persistent(kern, G, batch_threads(D), args, smem, bc.stream, false))) return rc;
+        if (!clustered.empty()) {
+            // one cluster per cloud, cl CTAs of at most cap_max pieces each
+            BatchArgs b = a;
+            b.order = d_order + small.size();
+            b.n_items = (uint32_t)clustered.size();
+            b.queue = d_queue + 1;
+            b.cap = cap_max;
+            b.mcap = 0;
+            void* args[] = {&b};
+            if ((rc = launch_clustered(cl_kern, (int)clustered.size(), cl, batch_threads(D), args,
+                                       cl_smem, bc.stream)))
+                return rc;
+        }
+        if (!small.empty()) {
+            a.order = d_order;
+            a.n_items = (uint32_t)small.size();
+            a.queue = d_queue;
+            a.cap = cap;
+            // what the piece starts and max coordinates leave of shared memory
+            // holds small clouds' points
+            uint64_t max_nc = 0;
+            for (uint32_t c : small) max_nc = std::max<uint64_t>(max_nc, bc.off[c + 1] - bc.off[c]);
+            const size_t left = avail - batch_smem_bytes(D, cap, 0);
+            a.mcap = (uint32_t)std::min<uint64_t>(left / (4 * D + 8), max_nc);
+            const size_t smem = batch_smem_bytes(D, cap, a.mcap);
+            const void* kern = bc.kd ? (const void*)batch_sample<D, FMA, true, false>
+                                     : (const void*)batch_sample<D, FMA, false, false>;
+            FPSGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem));
+            int per_sm = 0;
+            FPSGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, batch_threads(D), smem));
+            const int G = (int)std::min<uint64_t>(small.size(), (uint64_t)std::max(1, per_sm) * bc.sms);
+            void* args[] = {&a};
+            if ((rc = launch_persistent(kern, G, batch_threads(D), args, smem, bc.stream, false)))
+                return rc;
+        }
         timer.end(bc.stream);
         unsigned long long h_cnt[2] = {0, 0};
         FPSGPU_CUDA_TRY(cudaMemcpyAsync(h_cnt, cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, bc.stream));
         FPSGPU_CUDA_TRY(cudaStreamSynchronize(bc.stream));
         uint64_t ks = 0;
         for (uint32_t c : small) ks += bc.k[c];
+        for (uint32_t c : clustered) ks += bc.k[c];
         const uint64_t cn[2] = {h_cnt[0], h_cnt[1]};
         timer.finish(ks, cn);
     }

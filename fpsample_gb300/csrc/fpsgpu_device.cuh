@@ -102,6 +102,44 @@ __device__ __forceinline__ uint64_t warp_max_key(uint64_t k) {
     return ((uint64_t)mh << 32) | ml;
 }
 
+// ---- thread-block clusters: rank, barrier, distributed shared memory --------
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cluster_size() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+// Every thread of every CTA of the cluster: release what this thread wrote
+// (shared, distributed shared and global), wait for all, acquire.
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
+                     : "memory");
+}
+// Address of `p` (a shared variable of this CTA) in the shared memory of the
+// cluster's CTA `rank`.
+__device__ __forceinline__ uint32_t dsmem_addr(const void* p, uint32_t rank) {
+    uint32_t out;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+                 : "=r"(out)
+                 : "r"((uint32_t)__cvta_generic_to_shared(p)), "r"(rank));
+    return out;
+}
+__device__ __forceinline__ void dsmem_st_u64(uint32_t a, uint64_t v) {
+    asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(a), "l"(v) : "memory");
+}
+__device__ __forceinline__ void dsmem_st_f32(uint32_t a, float v) {
+    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t dsmem_ld_u32(uint32_t a) {
+    uint32_t v;
+    asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return v;
+}
+
 __device__ __forceinline__ void st_release_gpu(uint64_t* p, uint64_t v) {
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }

@@ -113,5 +113,10 @@ struct SamplerTimer {
 // cooperative launch helper: refuses grids that cannot be co-resident
 int launch_persistent(const void* func, int grid, int block, void** args, size_t smem,
                       cudaStream_t stream, bool cooperative);
+// thread-block cluster launches (batched engine's cluster sampler)
+int cluster_size_for_batch();
+int cluster_capacity(const void* func, int cl, int block, size_t smem, int* out);
+int launch_clustered(const void* func, int items, int cl, int block, void** args, size_t smem,
+                     cudaStream_t stream);
 
 }  // namespace fpsgpu

@@ -186,6 +186,8 @@ def test_gmm_1m_vanilla_prefix():
     np.testing.assert_array_equal(out[:256], ORACLE.fps(pts, 256, 0))
     t = tr.cpu().numpy()
     assert np.all(np.diff(t[1:]) <= 0)
+    # without a trace the call runs on a thread-block cluster: same indices
+    np.testing.assert_array_equal(fps.fps_sampling(pts, 16384, 0), out)
     assert len(np.unique(out)) == 16384
 
 
@@ -247,11 +249,36 @@ def test_batched_workload_sample_vs_oracle():
         np.testing.assert_array_equal(got[i], ORACLE.kdline(p, k, hs[i], 0))
 
 
-def test_cloud_beyond_shared_memory_uses_global_sampler(mode):
-    """1.2M points in 8 dimensions do not fit the grid's shared memory; the
-    global-memory sampler takes over and must give the same answer."""
+def test_cloud_beyond_shared_memory(mode):
+    """1.2M points in 8 dimensions: plain calls run on a thread-block cluster;
+    calls with a trace take the multi-CTA samplers, and these points do not fit
+    the grid's shared memory, so the global-memory sampler runs.  All must give
+    the oracle's answer."""
+    torch = pytest.importorskip("torch")
     rng = np.random.default_rng(21)
     pts = rng.random((1_200_000, 8), dtype=np.float32)
-    np.testing.assert_array_equal(fps.bucket_fps_kdline_sampling(pts, 1500, 6, 5),
-                                  ORACLE.kdline(pts, 1500, 6, 5, mode))
-    np.testing.assert_array_equal(fps.fps_sampling(pts, 300, 5), ORACLE.fps(pts, 300, 5, mode))
+    ref_kd = ORACLE.kdline(pts, 1500, 6, 5, mode)
+    ref_v = ORACLE.fps(pts, 300, 5, mode)
+    np.testing.assert_array_equal(fps.bucket_fps_kdline_sampling(pts, 1500, 6, 5), ref_kd)
+    np.testing.assert_array_equal(fps.fps_sampling(pts, 300, 5), ref_v)
+    t = torch.from_numpy(pts).cuda()
+    out, _ = capi.kdline_tensor(t, 1500, 6, 5, trace=True)
+    np.testing.assert_array_equal(out.cpu().numpy().astype(np.uint64), ref_kd)
+    out, _ = capi.fps_tensor(t, 300, 5, trace=True)
+    np.testing.assert_array_equal(out.cpu().numpy().astype(np.uint64), ref_v)
+
+
+@pytest.mark.parametrize("d", [2, 3, 6])
+def test_batch_with_several_cluster_clouds(d, mode):
+    # clouds with more pieces than one CTA holds each get a thread-block
+    # cluster; several of them share the cluster queue with small clouds
+    clouds, ks, hs, ss = _batch_clouds(30 + d, 5, 300, 3000, d)
+    rng = np.random.default_rng(d)
+    for n in (300_000, 520_000, 760_000):
+        clouds.append((rng.random((n, d)) * rng.uniform(1, 50, d)).astype(np.float32))
+        ks.append(1200)
+        hs.append(7)
+        ss.append(int(rng.integers(0, n)))
+    got = capi.kdline_batch(clouds, ks, hs, ss)
+    for p, k, h, s, g in zip(clouds, ks, hs, ss, got):
+        np.testing.assert_array_equal(g, ORACLE.kdline(p, k, h, s, mode))
