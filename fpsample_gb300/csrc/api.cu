@@ -104,6 +104,19 @@ int cluster_size_for_batch() {
     return v;
 }
 
+// FPSGPU_CLUSTER_MIN_PIECES: clouds with at least this many pieces run on a
+// cluster even when one CTA could hold them (0, the default: only clouds that
+// need it).  A tuning knob for batches whose largest clouds set the makespan.
+uint32_t cluster_min_pieces() {
+    static const uint32_t v = [] {
+        const char* e = std::getenv("FPSGPU_CLUSTER_MIN_PIECES");
+        if (!e) return 0u;
+        const long x = std::atol(e);
+        return x > 0 ? (uint32_t)x : 0u;
+    }();
+    return v;
+}
+
 // How many clusters of `cl` CTAs of `func` can be resident at once (0: none).
 int cluster_capacity(const void* func, int cl, int block, size_t smem, int* out) {
     *out = 0;

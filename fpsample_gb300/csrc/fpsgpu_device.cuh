@@ -119,6 +119,43 @@ __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
                      : "memory");
 }
+// mbarrier-completed remote stores: st.async writes into CTA `rank`'s shared
+// memory and counts its bytes on that CTA's mbarrier (no fence needed).
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"((uint32_t)__cvta_generic_to_shared(bar)),
+                 "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"((uint32_t)__cvta_generic_to_shared(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void st_async_u64(uint32_t addr, uint64_t v, uint32_t bar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(addr),
+                 "l"(v), "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void st_async_f32(uint32_t addr, float v, uint32_t bar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(addr),
+                 "r"(__float_as_uint(v)), "r"(bar)
+                 : "memory");
+}
 // Address of `p` (a shared variable of this CTA) in the shared memory of the
 // cluster's CTA `rank`.
 __device__ __forceinline__ uint32_t dsmem_addr(const void* p, uint32_t rank) {
@@ -127,12 +164,6 @@ __device__ __forceinline__ uint32_t dsmem_addr(const void* p, uint32_t rank) {
                  : "=r"(out)
                  : "r"((uint32_t)__cvta_generic_to_shared(p)), "r"(rank));
     return out;
-}
-__device__ __forceinline__ void dsmem_st_u64(uint32_t a, uint64_t v) {
-    asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(a), "l"(v) : "memory");
-}
-__device__ __forceinline__ void dsmem_st_f32(uint32_t a, float v) {
-    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
 }
 __device__ __forceinline__ uint32_t dsmem_ld_u32(uint32_t a) {
     uint32_t v;

@@ -63,6 +63,39 @@ class Scratch {
     std::vector<void*> ptrs_;
 };
 
+// A second stream that forks from and joins back into a caller's stream, for
+// two launches that should run side by side.  If it is dropped without a join
+// (an error path), it waits for its own work so that stream-ordered frees on
+// the caller's stream cannot overtake it.
+struct SideStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool joined = false;
+    SideStream() = default;
+    SideStream(const SideStream&) = delete;
+    SideStream& operator=(const SideStream&) = delete;
+    int fork(cudaStream_t from) {
+        FPSGPU_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        FPSGPU_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+        FPSGPU_CUDA_TRY(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+        FPSGPU_CUDA_TRY(cudaEventRecord(ev_fork, from));
+        FPSGPU_CUDA_TRY(cudaStreamWaitEvent(s, ev_fork, 0));
+        return FPSGPU_OK;
+    }
+    int join(cudaStream_t into) {
+        FPSGPU_CUDA_TRY(cudaEventRecord(ev_join, s));
+        FPSGPU_CUDA_TRY(cudaStreamWaitEvent(into, ev_join, 0));
+        joined = true;
+        return FPSGPU_OK;
+    }
+    ~SideStream() {
+        if (s && !joined) cudaStreamSynchronize(s);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (s) cudaStreamDestroy(s);
+    }
+};
+
 // One vanilla FPS call on device buffers.
 struct VanillaCall {
     const float* d_points;  // row-major [n][dim]
@@ -115,6 +148,7 @@ int launch_persistent(const void* func, int grid, int block, void** args, size_t
                       cudaStream_t stream, bool cooperative);
 // thread-block cluster launches (batched engine's cluster sampler)
 int cluster_size_for_batch();
+uint32_t cluster_min_pieces();
 int cluster_capacity(const void* func, int cl, int block, size_t smem, int* out);
 int launch_clustered(const void* func, int items, int cl, int block, void** args, size_t smem,
                      cudaStream_t stream);
