@@ -19,8 +19,22 @@ tree height picked per size class.  One step = all 256 clouds sampled.
   cpu_baseline  the oracle (C restatement of the reference, or the reference
           compiled from its sources where present) on a bounded sample, 1 core.
 
+Other workloads (--workload), each one of the reference's configurations:
+  gmm-1m            one 1,048,576-point Gaussian-mixture cloud, kd-line h=7,
+                    K=16,384
+  gmm-1m-vanilla    the same cloud, vanilla FPS
+  single-4k         vanilla FPS, 4,096 uniform points, K=1,024
+  large-16m         16,777,216 points, D=6, kd-line h=9, K=65,536
+  large-16m-vanilla the same cloud, vanilla FPS
+  served            a Poisson request stream into the request server
+Where the oracle cannot finish a cloud in seconds, the correctness check
+compares a prefix of the samples (FPS is prefix-stable in K) and the CPU
+numbers come from two truncated runs extrapolated linearly in K (said so in
+the line).
+
 --impl reference runs the reference's CPU implementation of the same path on
-all host cores (rank 0 only) and prints the same metric.
+all host cores (rank 0 only) and prints the same metric.  The reference is
+single-threaded per cloud, so a one-cloud workload uses one core.
 Multi-GPU (torchrun): replicas only -- every rank samples its own copy of the
 batch; value = all clouds / max step time over ranks ("weak" scaling).
 """
@@ -55,19 +69,44 @@ def h_for(n: int) -> int:
     return 9
 
 
-def workload(name: str):
+WORKLOADS = ["batched-256", "gmm-1m", "gmm-1m-vanilla", "single-4k", "large-16m",
+             "large-16m-vanilla", "served"]
+
+
+class Workload:
+    """algo: "kdline" or "vanilla"; clouds: [(points, k, h, start)]."""
+
+    def __init__(self, name, algo, clouds):
+        self.name, self.algo, self.clouds = name, algo, clouds
+        self.dim = int(clouds[0][0].shape[1])
+
+
+def workload(name: str) -> Workload:
     from fpsample_gb300 import workloads as W
 
     if name == "batched-256":
         clouds = W.batched_clouds(seed=W.SEEDS["batched-256"])
-        return [(p, k, h_for(p.shape[0]), 0) for p, k in clouds]
-    if name == "gmm-1m":
+        return Workload(name, "kdline", [(p, k, h_for(p.shape[0]), 0) for p, k in clouds])
+    if name in ("gmm-1m", "gmm-1m-vanilla"):
         p = W.gmm_cloud(1 << 20, seed=W.SEEDS["gmm-1m"])
-        return [(p, 16384, 7, 0)]
+        return Workload(name, "vanilla" if name.endswith("vanilla") else "kdline", [(p, 16384, 7, 0)])
     if name == "single-4k":
         p = W.uniform_cloud(4096, 3, seed=W.SEEDS["single-4k"])
-        return [(p, 1024, 5, 0)]
+        return Workload(name, "vanilla", [(p, 1024, 5, 0)])
+    if name in ("large-16m", "large-16m-vanilla"):
+        p = W.large_cloud(1 << 24, seed=W.SEEDS["large-16m"])
+        return Workload(name, "vanilla" if name.endswith("vanilla") else "kdline", [(p, 65536, 9, 0)])
     raise ValueError(name)
+
+
+def truncated_k(algo: str, n: int, k: int):
+    """None when the oracle finishes (n, k) in seconds; else the smaller K of
+    the two truncated runs (the other is twice as many samples)."""
+    if algo == "vanilla" and n * k > 5e8:
+        return max(8, min(k // 4, int(2e8 // n)))
+    if algo == "kdline" and n > (4 << 20):
+        return min(k // 4, 128)
+    return None
 
 
 def dist_env():
@@ -148,11 +187,32 @@ def _cpu_impl():
     return "port", O.Oracle()
 
 
-def _cpu_run(impl, obj, pts, k, h, start):
+def _cpu_run(impl, obj, algo, pts, k, h, start):
     mode = os.environ.get("FPSAMPLE_FP_MODE", "nofma")
+    if algo == "vanilla":
+        if impl == "reference":
+            return obj.fps_sampling(pts, k, start)
+        return obj.fps(pts, k, start, mode)
     if impl == "reference":
         return obj.bucket_fps_kdline_sampling(pts, k, h, start)
     return obj.kdline(pts, k, h, start, mode)
+
+
+def _cpu_cloud_seconds(impl, obj, algo, p, k, h, s):
+    """(seconds for one cloud, how it was obtained): measured, or extrapolated
+    linearly in K from two truncated runs."""
+    kt = truncated_k(algo, p.shape[0], k)
+    if kt is None:
+        t0 = time.perf_counter()
+        _cpu_run(impl, obj, algo, p, k, h, s)
+        return time.perf_counter() - t0, None
+    t = []
+    for kk in (kt, 2 * kt):
+        t0 = time.perf_counter()
+        _cpu_run(impl, obj, algo, p, kk, h, s)
+        t.append(time.perf_counter() - t0)
+    est = t[0] + (t[1] - t[0]) * (k - kt) / kt
+    return est, f"K={kt} and K={2 * kt} timed ({t[0]:.2f} s, {t[1]:.2f} s), extrapolated linearly to K={k}"
 
 
 _W = {}
@@ -160,31 +220,35 @@ _W = {}
 
 def _worker_init(name):
     sys.path.insert(0, ROOT)
-    _W["clouds"] = workload(name)
+    _W["wl"] = workload(name)
     _W["impl"], _W["obj"] = _cpu_impl()
 
 
 def _worker_run(i):
-    p, k, h, s = _W["clouds"][i]
-    _cpu_run(_W["impl"], _W["obj"], p, k, h, s)
-    return i
+    wl = _W["wl"]
+    p, k, h, s = wl.clouds[i % len(wl.clouds)]
+    return _cpu_cloud_seconds(_W["impl"], _W["obj"], wl.algo, p, k, h, s)
 
 
-def cpu_baseline(clouds, budget_s: float = 12.0):
+def cpu_baseline(wl: Workload, budget_s: float = 12.0):
     impl, obj = _cpu_impl()
     t0 = time.perf_counter()
     done = 0
     pts_done = 0
-    for p, k, h, s in clouds:
-        _cpu_run(impl, obj, p, k, h, s)
+    secs = 0.0
+    how = None
+    for p, k, h, s in wl.clouds:
+        dt, how = _cpu_cloud_seconds(impl, obj, wl.algo, p, k, h, s)
+        secs += dt
         done += 1
         pts_done += p.shape[0]
         if time.perf_counter() - t0 > budget_s:
             break
-    dt = time.perf_counter() - t0
-    return {"value": done / dt, "unit": UNIT, "cores": 1, "kind": impl,
-            "sample": f"first {done} of {len(clouds)} clouds ({pts_done} points), one thread, "
-                      f"{dt:.1f} s"}
+    sample = (f"first {done} of {len(wl.clouds)} clouds ({pts_done} points), one thread, "
+              f"{secs:.1f} s of {wl.algo}")
+    if how:
+        sample += f"; {how}"
+    return {"value": done / secs, "unit": UNIT, "cores": 1, "kind": impl, "sample": sample}
 
 
 def run_reference_arm(args):
@@ -193,39 +257,58 @@ def run_reference_arm(args):
         return
     import multiprocessing as mp
 
-    clouds = workload(args.workload)
+    wl = workload(args.workload)
+    clouds = wl.clouds
     impl, _ = _cpu_impl()
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
+    # the reference samples one cloud on one thread: a one-cloud workload
+    # cannot use more than one core
+    copies = 1
+    cores = min(cores, len(clouds))
     # largest clouds first so that the pool drains evenly
-    order = sorted(range(len(clouds)), key=lambda i: -clouds[i][0].shape[0] * clouds[i][1])
+    order = sorted(range(len(clouds) * copies),
+                   key=lambda i: -clouds[i % len(clouds)][0].shape[0] * clouds[i % len(clouds)][1])
+    big = any(truncated_k(wl.algo, p.shape[0], k) for p, k, _, _ in clouds)
+    warmup = 1 if big else args.warmup
+    steps = 1 if big else args.steps
+    how = None
     with ctx.Pool(cores, initializer=_worker_init, initargs=(args.workload,)) as pool:
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             list(pool.imap_unordered(_worker_run, order))
         times = []
-        for _ in range(args.steps):
+        for _ in range(steps):
             t0 = time.perf_counter()
-            list(pool.imap_unordered(_worker_run, order))
-            times.append(time.perf_counter() - t0)
+            out = list(pool.imap_unordered(_worker_run, order))
+            wall = time.perf_counter() - t0
+            how = next((h for _, h in out if h), None)
+            # a truncated run stands for the whole cloud: the step lasts as
+            # long as the busiest core's extrapolated work
+            times.append(max(wall, max(sec for sec, _ in out)) if how else wall)
     step = statistics.mean(times)
-    v = len(clouds) / step
+    v = len(clouds) * copies / step
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": step * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generators)",
-            "config": config_of(args.workload, clouds),
+            "config": config_of(wl),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": impl,
-                             "sample": f"all {len(clouds)} clouds per step, {cores} processes"},
+                             "sample": f"{copies} cop{'y' if copies == 1 else 'ies'} of all "
+                                       f"{len(clouds)} clouds per step, {cores} processes, "
+                                       f"{wl.algo}" + (f"; per cloud: {how}" if how else "")},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def config_of(name, clouds):
+def config_of(wl: Workload):
+    name, clouds = wl.name, wl.clouds
     ns = [p.shape[0] for p, _, _, _ in clouds]
-    return {"workload": name, "n_clouds": len(clouds), "points_total": int(sum(ns)),
-            "samples_total": int(sum(k for _, k, _, _ in clouds)), "dim": 3,
+    return {"workload": name, "algo": wl.algo, "n_clouds": len(clouds),
+            "points_total": int(sum(ns)),
+            "samples_total": int(sum(k for _, k, _, _ in clouds)), "dim": wl.dim,
             "k": "N//4" if name == "batched-256" else int(clouds[0][1]),
-            "h": "size class: 5 (<8K), 7 (<256K), 9" if name == "batched-256" else clouds[0][2],
+            "h": ("size class: 5 (<8K), 7 (<256K), 9" if name == "batched-256"
+                  else (clouds[0][2] if wl.algo == "kdline" else None)),
             "start_idx": 0, "l2": "flushed before every step (256 MiB write)",
             "parallelism": "replicas"}
 
@@ -247,7 +330,9 @@ def run_gpu_arm(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
 
-    clouds = workload(args.workload)
+    wl = workload(args.workload)
+    clouds = wl.clouds
+    D = wl.dim
     # inputs resident in HBM: one buffer, per-cloud views
     sizes = [p.shape[0] for p, _, _, _ in clouds]
     offs = np.concatenate([[0], np.cumsum(sizes)])
@@ -264,20 +349,33 @@ def run_gpu_arm(args):
     hs = [h for _, _, h, _ in clouds]
     ss = [s for _, _, _, s in clouds]
 
-    def step_device():
-        # the batched engine: every cloud in one call
-        capi.kdline_batch_device(base_pts, offs, 3, ks, hs, ss, base_out, sptr)
-
     def step_plain():
         # the plain form: one GPU call per cloud
         for i, (p, k, h, s) in enumerate(clouds):
-            capi.kdline_device(base_pts + int(offs[i]) * 12, sizes[i], 3, k, s, h,
-                               base_out + int(koffs[i]) * 8, 0, sptr)
+            if wl.algo == "vanilla":
+                capi.fps_device(base_pts + int(offs[i]) * 4 * D, sizes[i], D, k, [s],
+                                base_out + int(koffs[i]) * 8, 0, sptr)
+            else:
+                capi.kdline_device(base_pts + int(offs[i]) * 4 * D, sizes[i], D, k, s, h,
+                                   base_out + int(koffs[i]) * 8, 0, sptr)
+
+    def step_device():
+        if wl.algo == "vanilla":
+            step_plain()  # vanilla has no batched entry point: one call per cloud
+        else:
+            # the batched engine: every cloud in one call
+            capi.kdline_batch_device(base_pts, offs, D, ks, hs, ss, base_out, sptr)
 
     pcs = [p for p, _, _, _ in clouds]
 
     def step_e2e():
-        fps.bucket_fps_kdline_sampling_batch(pcs, ks, hs, ss)
+        if wl.algo == "vanilla":
+            for p, k, _, s in clouds:
+                fps.fps_sampling(p, k, s)
+        elif len(clouds) == 1:
+            fps.bucket_fps_kdline_sampling(pcs[0], ks[0], hs[0], ss[0])
+        else:
+            fps.bucket_fps_kdline_sampling_batch(pcs, ks, hs, ss)
 
     def barrier():
         torch.cuda.synchronize()
@@ -294,10 +392,18 @@ def run_gpu_arm(args):
     check_ids = sorted(set(i for i in (0, 1, len(clouds) // 2, int(np.argmax(sizes)))
                            if i < len(clouds)))
     bit_exact = True
+    checked_prefix = {}
     for i in check_ids:
         p, k, h, s = clouds[i]
-        want = orc.kdline(p, k, h, s, fps.get_fp_mode())
-        bit_exact &= bool(np.array_equal(res[koffs[i]:koffs[i + 1]], want))
+        kt = truncated_k(wl.algo, p.shape[0], k)
+        kc = k if kt is None else kt  # FPS is prefix-stable in K
+        if wl.algo == "vanilla":
+            want = orc.fps(p, kc, s, fps.get_fp_mode())
+        else:
+            want = orc.kdline(p, kc, h, s, fps.get_fp_mode())
+        bit_exact &= bool(np.array_equal(res[koffs[i]:koffs[i] + kc], want))
+        if kt is not None:
+            checked_prefix[i] = kc
 
     for _ in range(args.warmup):
         flush.zero_()
@@ -356,7 +462,7 @@ def run_gpu_arm(args):
 
     if rank == 0:
         launches = int(st["kernel_launches"])
-        d = 3
+        d = D
         alg_bytes = st["pieces_tested"] * (8 * d + 8) + st["points_touched"] * (4 * d + 8)
         per_launch_bytes = alg_bytes / max(1, st["sampler_launches"])
         per_launch_ms = st["sampler_ms"] / max(1, st["sampler_launches"])
@@ -367,32 +473,49 @@ def run_gpu_arm(args):
         except OSError:
             pass
         peak = peaks.get("hbm_gbs", 6800.0)
+        bound, peak_source = "hbm", "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"
+        vanilla_equiv = None
+        if wl.algo == "vanilla":
+            # vanilla-equivalent bytes: every running distance read and written
+            # and every point read once per sample, N (K-1) (4D + 8) B per cloud
+            veq = sum(p.shape[0] * (k - 1) * (4 * d + 8) for p, k, _, _ in clouds)
+            vanilla_equiv = {"bytes_per_step": veq, "gbs": veq / (ms / 1e3) / 1e9}
+            # a cloud that stays on chip is bounded by L2, not HBM
+            onchip = {}
+            try:
+                onchip = json.load(open(os.path.join(ROOT, "profiles", "peaks.json")))
+            except OSError:
+                pass
+            if host_all.nbytes * 2 <= 96 << 20 and onchip.get("l2_gbs"):
+                bound, peak = "l2", onchip["l2_gbs"]
+                peak_source = "profiles/peaks.json l2_gbs (bench.py --probe peaks)"
         traffic = None
         tpath = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tpath):
             tj = json.load(open(tpath)).get(args.workload)
             if tj:
                 traffic = tj.get("dram_bytes_per_launch")
-        cpu = cpu_baseline(clouds) if world == 1 or rank == 0 else None
+        cpu = cpu_baseline(wl) if world == 1 or rank == 0 else None
         lat = sorted(step_ms)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generators, fpsample_gb300.workloads)",
-            "config": config_of(args.workload, clouds),
+            "config": config_of(wl),
             "bit_exact_checked_clouds": check_ids, "bit_exact": bit_exact,
+            "bit_exact_prefix_checked": checked_prefix or None,
+            "vanilla_equivalent": vanilla_equiv,
             "plain_per_cloud": {"value": len(clouds) / (plain_ms / 1e3), "unit": UNIT,
                                 "ms_per_step": plain_ms, "identical_to_batched": plain_ok,
                                 "batched_speedup": plain_ms / ms},
             "e2e": {"value": e2e_v, "unit": UNIT,
                     "h2d_bytes_per_step": int(host_all.nbytes),
                     "d2h_bytes_per_step": int(koffs[-1]) * 8},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                          "kernel": "sampler", "alg_bytes_per_launch": per_launch_bytes,
-                         "launch_ms": per_launch_ms,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+                         "launch_ms": per_launch_ms, "peak_source": peak_source},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": launches,
@@ -504,25 +627,46 @@ def run_latency_probe(args):
     print(json.dumps({"probe": "latency", "results": res}), flush=True)
 
 
+def run_peaks_probe(args):
+    """Shared-memory and L2 read bandwidth of this GPU (the roofline of vanilla
+    FPS on clouds that stay on chip), best of five, beside the driver-measured
+    HBM figure."""
+    import torch
+
+    from fpsample_gb300 import capi
+
+    torch.cuda.init()
+    out = {"probe": "peaks", "device": torch.cuda.get_device_name(0)}
+    for level, key in ((0, "smem_gbs"), (1, "l2_gbs")):
+        out[key] = max(capi.measure_bandwidth(level) for _ in range(5))
+    try:
+        out["hbm_gbs"] = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, KeyError):
+        out["hbm_gbs"] = None
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="batched-256",
-                    choices=["batched-256", "gmm-1m", "single-4k", "served"])
+    ap.add_argument("--workload", default="batched-256", choices=WORKLOADS)
     ap.add_argument("--served-window", type=float, default=0.1,
                     help="seconds of the served request stream to replay")
     ap.add_argument("--small-workers", type=int, default=8)
     ap.add_argument("--large-workers", type=int, default=2)
-    ap.add_argument("--probe", default=None, choices=["latency"],
+    ap.add_argument("--probe", default=None, choices=["latency", "peaks"],
                     help="print a diagnostic table instead of the benchmark line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.probe == "latency":
         run_latency_probe(args)
+        return
+    if args.probe == "peaks":
+        run_peaks_probe(args)
         return
     if args.workload == "served" and args.impl != "reference":
         run_served(args)

@@ -25,7 +25,8 @@ LIB = os.path.join(HERE, "libfpsgpu.so")
 EXT = os.path.join(HERE, "_fpsample" + sysconfig.get_config_var("EXT_SUFFIX"))
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_UNITS = ["api", "vanilla_nofma", "vanilla_fma", "engine_nofma", "engine_fma", "noalloc", "server"]
+CU_UNITS = ["api", "vanilla_nofma", "vanilla_fma", "engine_nofma", "engine_fma", "noalloc", "server",
+            "peaks"]
 
 
 def _nvcc() -> str:

@@ -41,6 +41,7 @@ SIGNATURES = {
     "fpsgpu_stats_get": (None, [ctypes.c_void_p]),
     "fpsgpu_stats_timing": (None, [ctypes.c_int]),
     "fpsgpu_last_error": (ctypes.c_char_p, []),
+    "fpsgpu_measure_bandwidth": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "fpsgpu_version": (ctypes.c_char_p, []),
 }
 
@@ -282,3 +283,10 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def measure_bandwidth(level: int) -> float:
+    """Read bandwidth in GB/s of an on-chip level: 0 shared memory, 1 L2."""
+    v = ctypes.c_double(0.0)
+    _check("fpsgpu_measure_bandwidth", lib().fpsgpu_measure_bandwidth(level, ctypes.byref(v)))
+    return v.value

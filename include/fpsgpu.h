@@ -189,6 +189,13 @@ const char *fpsgpu_last_error(void);
 /* library version string */
 const char *fpsgpu_version(void);
 
+/* ---- diagnostics (no reference counterpart) -------------------------------
+ * Read bandwidth of an on-chip level of the current GPU, in GB/s, measured by a
+ * short microbenchmark: level 0 = shared memory (all SMs together), level 1 =
+ * L2 (a 32 MB buffer).  The roofline of vanilla FPS on clouds that stay on
+ * chip.  Synchronous; allocates and frees its own buffers. */
+int fpsgpu_measure_bandwidth(int level, double *gbs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -191,6 +191,24 @@ def test_gmm_1m_vanilla_prefix():
     assert len(np.unique(out)) == 16384
 
 
+def test_large_16m_d6_prefixes():
+    """large-16m workload at full size (N=16,777,216, D=6, K=65,536): kd-line
+    h=9 and vanilla run to full K on the GPU; the oracle checks prefixes (FPS
+    is prefix-stable in K), and the kd-line fp32 trace never increases."""
+    torch = pytest.importorskip("torch")
+    pts = W.large_cloud(1 << 24, seed=W.SEEDS["large-16m"])
+    t = torch.from_numpy(pts).cuda()
+    kd = fps.bucket_fps_kdline_sampling(pts, 65536, 9, 0)
+    np.testing.assert_array_equal(kd[:128], ORACLE.kdline(pts, 128, 9, 0))
+    assert len(np.unique(kd)) == 65536
+    out, tr = capi.kdline_tensor(t, 65536, 9, 0, trace=True)
+    np.testing.assert_array_equal(out.cpu().numpy().astype(np.uint64), kd)
+    assert np.all(np.diff(tr.cpu().numpy()[1:]) <= 0)
+    v = fps.fps_sampling(pts, 65536, 0)
+    np.testing.assert_array_equal(v[:12], ORACLE.fps(pts, 12, 0))
+    assert len(np.unique(v)) == 65536
+
+
 def _batch_clouds(seed, count, lo, hi, d=3):
     rng = np.random.default_rng(seed)
     clouds, ks, hs, ss = [], [], [], []
