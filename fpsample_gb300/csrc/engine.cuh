@@ -631,7 +631,7 @@ __global__ void __launch_bounds__(kSampleThreads, 1) fps_sample(SampleArgs a) {
 // Recomputes one dirty piece [ps, pe) against reference point r: running
 // distances lowered with the reference's strict "<" rule (or initialised to
 // min(init, d) on the first pass) and the piece's new max key (returned to the
-// whole warp).  The one lane holding the max point (keys are unique) writes its
+// whole warp; batch_key when BK, else make_key).  The one lane holding the max point (keys are unique) writes its
 // coordinates to c_base[d * c_stride]; no shuffles.  xb/disb/tagb may point to
 // shared or global memory; xs is the coordinate stride.  Pieces of at most
 // kPiece points take an unrolled path that issues every load of the piece
@@ -654,7 +654,7 @@ __device__ __forceinline__ uint32_t batch_key_pos(uint64_t key) {
     return KD ? m - f : f;
 }
 
-template <int D, bool FMA, bool KD>
+template <int D, bool FMA, bool KD, bool BK = true>
 __device__ __forceinline__ uint64_t recompute_piece(const float* xb, uint64_t xs, float* disb,
                                                     const uint32_t* tagb, uint32_t ps, uint32_t pe,
                                                     const float* r, bool first, float* c_base,
@@ -687,7 +687,7 @@ __device__ __forceinline__ uint64_t recompute_piece(const float* xb, uint64_t xs
                 float v = dv[j];
                 if (dd < v) v = dd;
                 if (first || dd < dv[j]) disb[p] = v;
-                const uint64_t kk = batch_key<KD>(v, tg[j] - tag_base, q);
+                const uint64_t kk = BK ? batch_key<KD>(v, tg[j] - tag_base, q) : make_key<KD>(v, tg[j]);
                 if (kk > pk) {
                     pk = kk;
 #pragma unroll
@@ -705,7 +705,7 @@ __device__ __forceinline__ uint64_t recompute_piece(const float* xb, uint64_t xs
             float v = old;
             if (dd < v) v = dd;
             if (first || dd < old) disb[p] = v;
-            const uint64_t kk = batch_key<KD>(v, tagb[p] - tag_base, q);
+            const uint64_t kk = BK ? batch_key<KD>(v, tagb[p] - tag_base, q) : make_key<KD>(v, tagb[p]);
             if (kk > pk) {
                 pk = kk;
 #pragma unroll
@@ -1011,6 +1011,182 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
             atomicAdd(a.counters, tested);
             atomicAdd(a.counters + 1, touched);
         }
+    }
+}
+
+// ---- one cloud on the whole grid, piece records in registers ----------------
+//
+// For clouds whose points fit neither one SM nor a cluster (e.g. 16.7M points):
+// a persistent cooperative grid of G CTAs.  Piece q of the range belongs to CTA
+// q mod G (neighbouring pieces, which turn dirty together, land in different
+// CTAs), and there to slot j of thread lane, warp exactly as in batch_sample;
+// boxes and keys live in registers, points and running distances in HBM/L2.
+// Per sample: tests, recompute of the dirty pieces (recompute_piece, plain
+// 32-bit-tag keys: positions may exceed batch_key's 21 bits), each warp offers
+// its max key and piece, one __syncthreads, warp 0 takes the CTA's max and that
+// piece's max coordinates into exchange_leader (the grid-wide argmax with the
+// winner's coordinates), one __syncthreads.  Forced samples and the trace work
+// as in fps_sample.  At most G x kRegThreads x kRegSlots pieces.
+constexpr int kRegThreads = 512;
+constexpr int kRegSlots = 4;
+constexpr uint32_t kRegCap = (uint32_t)kRegThreads * kRegSlots;
+
+inline size_t grid_reg_smem_bytes(int D) { return (size_t)kRegCap * (8 + 4 * D); }
+
+template <int D, bool FMA, bool KD>
+__global__ void __launch_bounds__(kRegThreads, 1) grid_sample_reg(SampleArgs a) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    constexpr uint32_t cap = kRegCap;
+    uint32_t* s_ps = reinterpret_cast<uint32_t*>(s_dyn);  // [cap] my pieces' starts
+    uint32_t* s_pe = s_ps + cap;                           // [cap] and ends
+    float* s_mc = reinterpret_cast<float*>(s_pe + cap);    // [D][cap] max coordinates
+    __shared__ uint64_t s_wkey[32];
+    __shared__ uint32_t s_wq[32];
+    __shared__ float s_ref[kMaxDim];
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const uint32_t T = blockDim.x, G = gridDim.x, rank = blockIdx.x;
+    const uint64_t n = a.n;
+    const uint32_t np = a.npieces ? *a.npieces : a.np_fixed;
+    const uint32_t nmine = np > rank ? (np - rank + G - 1) / G : 0u;
+
+    float lo[kRegSlots][D], hi[kRegSlots][D];
+    uint64_t key[kRegSlots];
+    uint32_t myq[kRegSlots];
+#pragma unroll
+    for (int j = 0; j < kRegSlots; ++j) {
+        myq[j] = (uint32_t)j * T + (uint32_t)lane * nwarps + warp;
+        key[j] = 0;
+        const bool have = myq[j] < nmine;
+        const uint64_t q = (uint64_t)myq[j] * G + rank;
+        // an empty slot gets an inverted box: never nearer than its key 0
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            lo[j][d] = have ? a.plo[q * D + d] : INFINITY;
+            hi[j][d] = have ? a.phi[q * D + d] : -INFINITY;
+        }
+    }
+    for (uint32_t i = tid; i < nmine; i += T) {
+        const uint64_t q = (uint64_t)i * G + rank;
+        s_ps[i] = a.pstart[q];
+        s_pe[i] = a.pstart[q + 1];
+    }
+    const uint32_t tag0 = (uint32_t)a.forced[0];
+    if (tid < D) s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
+    if (tid == 0) s_abort = 0;
+    // outputs hold tags while sampling; kd-line tags are mapped afterwards
+    if (rank == 0 && tid == 0 && a.k > 0) {
+        a.out[0] = KD ? tag0 : tag0 - a.id_offset;
+        if (a.trace) a.trace[0] = KD ? FLT_MAX : INFINITY;
+    }
+    __syncthreads();
+
+    unsigned long long tested = 0, touched = 0;
+    {
+        uint32_t mine = 0;
+#pragma unroll
+        for (int j = 0; j < kRegSlots; ++j) mine += myq[j] < nmine ? 1u : 0u;
+        if (a.k > 2) tested += (unsigned long long)mine * (a.k - 2);
+    }
+    uint32_t xround = 0;
+    uint64_t lbest = 0, wbest = 0;  // my best key; the warp's (warp-uniform)
+    uint32_t lbq = 0, wq = 0;       // and their pieces
+    for (uint64_t t = 0; t + 1 < a.k; ++t) {
+        float r[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) r[d] = s_ref[d];
+        const bool first = t == 0;
+        uint32_t dm = 0;
+#pragma unroll
+        for (int j = 0; j < kRegSlots; ++j) {
+            const bool dj = first ? myq[j] < nmine
+                                  : box_bound<D, FMA>(lo[j], hi[j], r) < key_dist(key[j]);
+            dm |= (uint32_t)dj << j;
+        }
+        if (__any_sync(kFull, dm != 0)) {
+#pragma unroll
+            for (int j = 0; j < kRegSlots; ++j) {
+                uint32_t m = __ballot_sync(kFull, (dm >> j) & 1u);
+                while (m) {
+                    const int l = __ffs(m) - 1;
+                    m &= m - 1;
+                    const uint32_t q = __shfl_sync(kFull, myq[j], l);
+                    const uint32_t ps = s_ps[q], pe = s_pe[q];
+                    if (lane == 0) touched += pe - ps;
+                    const uint64_t wk = recompute_piece<D, FMA, KD, false>(
+                        a.X, n, a.dis, a.tag, ps, pe, r, first, s_mc + q, cap, 0u, q);
+                    if (lane == l) key[j] = wk;
+                }
+            }
+            if (dm) {
+                lbest = 0;
+#pragma unroll
+                for (int j = 0; j < kRegSlots; ++j) {
+                    if (key[j] > lbest) {
+                        lbest = key[j];
+                        lbq = myq[j];
+                    }
+                }
+            }
+            wbest = warp_max_key(lbest);
+            const int ow = __ffs(__ballot_sync(kFull, wbest != 0 && lbest == wbest)) - 1;
+            wq = __shfl_sync(kFull, lbq, ow < 0 ? 0 : ow);
+        }
+        const bool forced = t + 1 < a.n_forced;
+        if (lane == 0) {
+            s_wkey[warp] = wbest;
+            s_wq[warp] = wq;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            uint64_t g = 0;
+            uint32_t tg;
+            bool ok = true;
+            float wc[D];
+            if (forced) {
+                tg = (uint32_t)a.forced[t + 1];
+#pragma unroll
+                for (int d = 0; d < D; ++d) wc[d] = a.Xref[(uint64_t)d * n + tg];
+            } else {
+                const uint64_t kw = lane < nwarps ? s_wkey[lane] : 0ull;
+                g = warp_max_key(kw);
+                const int w = __ffs(__ballot_sync(kFull, lane < nwarps && kw == g)) - 1;
+                const uint32_t qw = s_wq[w];
+                float mc[D];
+#pragma unroll
+                for (int d = 0; d < D; ++d) mc[d] = g != 0 ? s_mc[(size_t)d * cap + qw] : 0.0f;
+                if (G > 1) {
+                    g = exchange_leader<D>(a.slots, a.slots + (uint64_t)G * leader_words<D>(), G,
+                                           xround++, g, mc, wc, a.err);
+                } else {
+#pragma unroll
+                    for (int d = 0; d < D; ++d) wc[d] = mc[d];
+                }
+                ok = g != 0;
+                tg = key_pos<KD>(g);
+            }
+            if (ok && tg >= n) {
+                ok = false;
+                if (lane == 0) atomicOr(a.err, kErrBadIndex);
+            }
+            if (!ok) {
+                if (lane == 0) s_abort = 1;
+            } else {
+#pragma unroll
+                for (int d = 0; d < D; ++d)
+                    if (lane == d) s_ref[d] = wc[d];  // static indices keep wc in registers
+                if (rank == 0 && lane == 0) {
+                    a.out[t + 1] = KD ? tg : tg - a.id_offset;
+                    if (a.trace) a.trace[t + 1] = forced ? INFINITY : key_dist(g);
+                }
+            }
+        }
+        __syncthreads();
+        if (s_abort) break;
+    }
+    if (a.counters && lane == 0) {
+        atomicAdd(a.counters, tested);
+        atomicAdd(a.counters + 1, touched);
     }
 }
 
@@ -1529,16 +1705,25 @@ int sample_grid(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint32_t 
     int rc = sample_grid_smem<D, FMA>(bt, n, kd, piece0, np, k, h_forced, n_forced, id_offset,
                                       d_out, d_trace, stream, sms, sc);
     if (rc != kNoFit) return rc;
+    uint32_t h_np = np;
+    if (np == ~0u) {
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(&h_np, bt.d_np, 4, cudaMemcpyDeviceToHost, stream));
+        FPSGPU_CUDA_TRY(cudaStreamSynchronize(stream));
+    }
+    // registers hold the piece records when the grid has room for them
+    const uint64_t g_reg = std::min<uint64_t>((uint64_t)sms, (uint64_t)kMaxGridCoords);
+    const bool reg = h_np <= g_reg * kRegCap;
     float* dis;
-    uint64_t* pkey;
+    uint64_t* pkey = nullptr;
     const uint64_t nkeys = np == ~0u ? bt.np_cap : np;
     if ((rc = sc.alloc(&dis, n))) return rc;
-    if ((rc = sc.alloc(&pkey, nkeys))) return rc;
+    if (!reg && (rc = sc.alloc(&pkey, nkeys))) return rc;
     // grid: about two pieces per warp (pieces hold ~kPiece/2..kPiece points)
     uint64_t G = (points_in_range / (kPiece / 2) + 63) / 64;
     G = std::max<uint64_t>(1, std::min<uint64_t>({G, (uint64_t)sms, (uint64_t)kMaxGridCoords}));
+    if (reg) G = std::max<uint64_t>(1, std::min<uint64_t>(g_reg, (h_np + 127) / 128));
     uint64_t* slots;
-    const uint64_t nslots = (G + 1) * leader_words<0>();
+    const uint64_t nslots = (G + 1) * (reg ? leader_words<D>() : leader_words<0>());
     if ((rc = sc.alloc(&slots, nslots))) return rc;
     FPSGPU_CUDA_TRY(cudaMemsetAsync(slots, 0, nslots * sizeof(uint64_t), stream));
     uint64_t* d_forced;
@@ -1574,8 +1759,16 @@ int sample_grid(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint32_t 
     void* args[] = {&s};
     SamplerTimer timer;
     timer.begin(stream);
-    const void* kern = kd ? (const void*)fps_sample<D, FMA, true> : (const void*)fps_sample<D, FMA, false>;
-    if ((rc = launch_persistent(kern, (int)G, kSampleThreads, args, 0, stream, G > 1))) return rc;
+    if (reg) {
+        const void* kern = kd ? (const void*)grid_sample_reg<D, FMA, true>
+                              : (const void*)grid_sample_reg<D, FMA, false>;
+        const size_t smem = grid_reg_smem_bytes(D);
+        FPSGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if ((rc = launch_persistent(kern, (int)G, kRegThreads, args, smem, stream, G > 1))) return rc;
+    } else {
+        const void* kern = kd ? (const void*)fps_sample<D, FMA, true> : (const void*)fps_sample<D, FMA, false>;
+        if ((rc = launch_persistent(kern, (int)G, kSampleThreads, args, 0, stream, G > 1))) return rc;
+    }
     timer.end(stream);
     if (kd) {
         stats_count_launch();

@@ -209,6 +209,18 @@ def test_large_16m_d6_prefixes():
     assert len(np.unique(v)) == 65536
 
 
+def test_beyond_register_capacity_uses_streaming_sampler():
+    """33.5M points in one dimension: more pieces than the whole grid holds in
+    registers, so the streaming sampler (piece records in HBM) runs."""
+    rng = np.random.default_rng(33)
+    pts = rng.random((1 << 25, 1), dtype=np.float32)
+    v = fps.fps_sampling(pts, 64, 7)
+    np.testing.assert_array_equal(v[:8], ORACLE.fps(pts, 8, 7))
+    assert len(np.unique(v)) == 64
+    kd = fps.bucket_fps_kdline_sampling(pts, 64, 1, 7)
+    np.testing.assert_array_equal(kd[:24], ORACLE.kdline(pts, 24, 1, 7))
+
+
 def _batch_clouds(seed, count, lo, hi, d=3):
     rng = np.random.default_rng(seed)
     clouds, ks, hs, ss = [], [], [], []
