@@ -624,6 +624,8 @@ def run_latency_probe(args):
     res["gmm1m_kdline_h7"] = {"ms": dt * 1e3, "us_per_sample": dt * 1e6 / 16384}
     dt = best_of(lambda: capi.fps_device(g.data_ptr(), 1 << 20, 3, 16384, [0], out.data_ptr(), 0, s))
     res["gmm1m_vanilla"] = {"ms": dt * 1e3, "us_per_sample": dt * 1e6 / 16384}
+    dt = best_of(lambda: capi.kdtree_tensor(g, 16384, 0))
+    res["gmm1m_kdtree"] = {"ms": dt * 1e3, "us_per_sample": dt * 1e6 / 16384}
     print(json.dumps({"probe": "latency", "results": res}), flush=True)
 
 

@@ -1,10 +1,11 @@
 """fpsample_gb300: farthest point sampling on NVIDIA GB300, a drop-in for fpsample.
 
-``import fpsample_gb300 as fpsample`` and keep calling ``fps_sampling`` and
-``bucket_fps_kdline_sampling`` with the same numpy arrays, ``n_samples``, ``h``
-and ``start_idx``: the returned uint64 index arrays are identical to the
-reference CPU library's.  The argument checks below are the reference's own
-(reference ``src/fpsample/__init__.py:19-65`` and ``:174-206``), including their
+``import fpsample_gb300 as fpsample`` and keep calling ``fps_sampling``,
+``bucket_fps_kdline_sampling`` and ``bucket_fps_kdtree_sampling`` with the same
+numpy arrays, ``n_samples``, ``h`` and ``start_idx``: the returned uint64 index
+arrays are identical to the reference CPU library's.  The argument checks below
+are the reference's own (reference ``src/fpsample/__init__.py:19-65``,
+``:145-171`` and ``:174-206``), including their
 ``AssertionError`` messages and the random start drawn from numpy's global
 ``np.random`` state when ``start_idx`` is None.
 
@@ -168,8 +169,36 @@ def fps_npdu_kdtree_sampling(pc, n_samples, w=None, start_idx=None):
     return _fps_npdu_kdtree_sampling(pc, n_samples, w, start_idx)
 
 
-def bucket_fps_kdtree_sampling(pc, n_samples, start_idx=None):
-    """Not part of the GB300 build (full kd-tree QuickFPS); raises NotImplementedError."""
+def bucket_fps_kdtree_sampling(
+    pc: np.ndarray, n_samples: int, start_idx: Optional[Union[int, List[int]]] = None
+) -> np.ndarray:
+    """
+    Bucket-based FPS sampling using KDTree. Also called "QuickFPS" in the paper.
+
+    Args:
+        pc (np.ndarray): The input point cloud of shape (n_pts, D).
+        n_samples (int): Number of samples.
+        start_idx (int or list[int], default=None): The starting index of sampling. If set to None, it will be randomly picked.
+            If multiple start indices are given, they are used as a start set for the FPS and will all be present in the final samples.
+    Returns:
+        np.ndarray: The selected indices of shape (n_samples,).
+
+    Same checks and results as the reference (src/fpsample/__init__.py:145-171),
+    computed on the GPU: the kd-line engine with no height limit and ties to
+    the last position of the tree's order (KDNode.h:41-46).
+    """
+    assert n_samples >= 1, "n_samples should be >= 1"
+    assert pc.ndim == 2
+    n_pts, _ = pc.shape
+    assert n_pts >= n_samples, "n_pts should be >= n_samples"
+    assert (
+        start_idx is None or 0 <= start_idx < n_pts
+    ), "start_idx should be None or 0 <= start_idx < n_pts"
+    if isinstance(start_idx, list):
+        assert len(start_idx) <= n_samples, "len(start_idx) should be <= n_samples"
+    pc = np.ascontiguousarray(pc, dtype=np.float32)
+    # Random pick a start if not given
+    start_idx = get_start_idx(n_pts, start_idx)
     return _bucket_fps_kdtree_sampling(pc, n_samples, start_idx)
 
 

@@ -23,6 +23,8 @@ _szp = ctypes.POINTER(ctypes.c_size_t)
 # name -> (restype, argtypes)
 SIGNATURES = {
     "bucket_fps_kdline": (ctypes.c_int, [_f32p, _sz, _sz, _sz, _sz, _sz, _szp]),
+    "bucket_fps_kdtree": (ctypes.c_int, [_f32p, _sz, _sz, _sz, _sz, _szp]),
+    "fpsgpu_kdtree_device": (ctypes.c_int, [_vp, _sz, _sz, _sz, _sz, _vp, _vp, _vp]),
     "fpsgpu_fps": (ctypes.c_int, [_f32p, _sz, _sz, _sz, _szp, _sz, _szp]),
     "fpsgpu_kdline_device": (ctypes.c_int, [_vp, _sz, _sz, _sz, _sz, _sz, _vp, _vp, _vp]),
     "fpsgpu_fps_device": (ctypes.c_int, [_vp, _sz, _sz, _sz, _szp, _sz, _vp, _vp, _vp]),
@@ -124,6 +126,34 @@ def bucket_fps_kdline(pc, n_samples: int, start_idx: int, height: int) -> np.nda
                                  start_idx, height, out.ctypes.data_as(_szp))
     _check("bucket_fps_kdline", rc)
     return out
+
+
+def bucket_fps_kdtree(pc, n_samples: int, start_idx: int) -> np.ndarray:
+    """The reference-compatible kd-tree C entry point, host buffers."""
+    a = _rows(pc)
+    out = np.zeros(n_samples, np.uint64)
+    rc = lib().bucket_fps_kdtree(a.ctypes.data_as(_f32p), a.shape[0], a.shape[1], n_samples,
+                                 start_idx, out.ctypes.data_as(_szp))
+    _check("bucket_fps_kdtree", rc)
+    return out
+
+
+def kdtree_tensor(points, n_samples: int, start_idx: int = 0, trace: bool = False):
+    """bucket_fps_kdtree on a torch CUDA tensor [N, D] float32; int64 CUDA tensor out."""
+    import torch
+
+    pts = points.contiguous()
+    if pts.dtype != torch.float32 or not pts.is_cuda or pts.dim() != 2:
+        raise ValueError("points must be a 2D float32 CUDA tensor")
+    out = torch.empty(n_samples, dtype=torch.int64, device=pts.device)
+    tr = torch.empty(n_samples, dtype=torch.float32, device=pts.device) if trace else None
+    with torch.cuda.device(pts.device):
+        stream = torch.cuda.current_stream().cuda_stream
+        _check("fpsgpu_kdtree_device",
+               lib().fpsgpu_kdtree_device(pts.data_ptr(), pts.shape[0], pts.shape[1], n_samples,
+                                          start_idx, out.data_ptr(), tr.data_ptr() if trace else 0,
+                                          stream))
+    return (out, tr) if trace else out
 
 
 def fps(pc, n_samples: int, starts) -> np.ndarray:

@@ -384,8 +384,10 @@ int resolve_stream(void* stream, DevCtx* ctx, cudaStream_t* out) {
 // per sample up to ~250K points); a larger cloud falls through to the same
 // multi-CTA sampler run_engine uses.  Results are identical either way.
 int single_via_batch(const float* d_points, size_t n, size_t dim, size_t k, size_t start,
-                     size_t height, bool kd, uint64_t* d_out, cudaStream_t stream, int sms) {
+                     size_t height, bool kd, uint64_t* d_out, cudaStream_t stream, int sms,
+                     bool tie_last = false) {
     BatchCall b;
+    b.tie_last = tie_last;
     b.d_points = d_points;
     b.off = {0, (uint64_t)n};
     b.k = {(uint64_t)k};
@@ -452,12 +454,17 @@ int check_kdline_args(size_t n, size_t dim, size_t start) {
     return FPSGPU_OK;
 }
 
+// tie_last: bucket_fps_kdtree, the same engine with no height limit and ties
+// to the last position of the tree's order.
 int kdline_device_impl(const float* d_points, size_t n, size_t dim, size_t k, size_t start,
-                       size_t height, uint64_t* d_out, float* d_trace, cudaStream_t stream, int sms) {
+                       size_t height, uint64_t* d_out, float* d_trace, cudaStream_t stream, int sms,
+                       bool tie_last = false) {
     if (d_trace == nullptr)
-        return single_via_batch(d_points, n, dim, k, start, height, true, d_out, stream, sms);
+        return single_via_batch(d_points, n, dim, k, start, height, true, d_out, stream, sms,
+                                tie_last);
     const uint64_t forced = start;
     EngineCall c{};
+    c.tie_last = tie_last;
     c.d_points = d_points;
     c.n = n;
     c.k = k;
@@ -572,6 +579,43 @@ int bucket_fps_kdline(const float* raw_data, size_t n_points, size_t dim, size_t
                                     cudaMemcpyHostToDevice, ctx.stream));
     if ((rc = kdline_device_impl(d_pts, n_points, dim, n_samples, start_idx, height, d_out, nullptr,
                                  ctx.stream, ctx.sms)))
+        return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(sampled_point_indices, d_out, n_samples * sizeof(uint64_t),
+                                    cudaMemcpyDeviceToHost, ctx.stream));
+    FPSGPU_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
+    return FPSGPU_OK;
+}
+
+int fpsgpu_kdtree_device(const float* d_points, size_t n_points, size_t dim, size_t n_samples,
+                         size_t start_idx, uint64_t* d_out, float* d_trace, void* stream) {
+    clear_error();
+    int rc = check_kdline_args(n_points, dim, start_idx);
+    if (rc) return rc;
+    if (n_samples == 0) return FPSGPU_OK;
+    DevCtx ctx;
+    cudaStream_t s;
+    if ((rc = resolve_stream(stream, &ctx, &s))) return rc;
+    return kdline_device_impl(d_points, n_points, dim, n_samples, start_idx, ~(size_t)0, d_out,
+                              d_trace, s, ctx.sms, true);
+}
+
+int bucket_fps_kdtree(const float* raw_data, size_t n_points, size_t dim, size_t n_samples,
+                      size_t start_idx, size_t* sampled_point_indices) {
+    clear_error();
+    int rc = check_kdline_args(n_points, dim, start_idx);
+    if (rc) return rc;
+    if (n_samples == 0) return FPSGPU_OK;
+    DevCtx ctx;
+    if ((rc = current_ctx(&ctx))) return rc;
+    Scratch sc(ctx.stream);
+    float* d_pts;
+    uint64_t* d_out;
+    if ((rc = sc.alloc(&d_pts, n_points * dim))) return rc;
+    if ((rc = sc.alloc(&d_out, n_samples))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_pts, raw_data, n_points * dim * sizeof(float),
+                                    cudaMemcpyHostToDevice, ctx.stream));
+    if ((rc = kdline_device_impl(d_pts, n_points, dim, n_samples, start_idx, ~(size_t)0, d_out,
+                                 nullptr, ctx.stream, ctx.sms, true)))
         return rc;
     FPSGPU_CUDA_TRY(cudaMemcpyAsync(sampled_point_indices, d_out, n_samples * sizeof(uint64_t),
                                     cudaMemcpyDeviceToHost, ctx.stream));

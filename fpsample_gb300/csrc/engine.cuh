@@ -75,7 +75,19 @@ struct BuildArgs {
     uint32_t* refine_cnt;
     uint64_t n;
     int* err;
+    // sampling builds: a node of at most kPiece points starts one piece and its
+    // subtree (still split exactly) starts no more; build-only calls keep the
+    // reference's buckets (every exact leaf starts one)
+    int coarse;
+    // bucket_fps_kdtree: the snapshot gives every point the REVERSED position
+    // of its cloud as tag, so that "lowest tag wins" means "last position wins"
+    int reverse;
+    const uint64_t* cloud_off;  // [n_clouds + 1] (reverse only)
+    uint32_t n_clouds;
 };
+
+// Node depth word: bit 31 marks a node inside an existing piece (coarse mode).
+constexpr uint32_t kCovered = 0x80000000u;
 
 // Block-wide exclusive rank of `f` among the block's threads (thread order),
 // and the block total.  `s_w` is a 2 x 32 array that alternates between calls
@@ -138,7 +150,9 @@ __global__ void build_prepare(const float* __restrict__ pts, BuildArgs a, const 
         if (len == 0) continue;
         a.flag[root.x] = 1;  // every cloud starts a piece
         if (exact && root.w > 0 && len > 1) {
-            a.cur[atomicAdd(a.cnt_cur, 1u)] = root;
+            uint4 r = root;
+            if (a.coarse && len <= kPiece) r.z |= kCovered;  // the whole cloud is one piece
+            a.cur[atomicAdd(a.cnt_cur, 1u)] = r;
         } else if (len > kPiece) {
             a.refine[atomicAdd(a.refine_cnt, 1u)] = root;
         }
@@ -376,34 +390,56 @@ __global__ void __launch_bounds__(EXACT ? kBuildThreads : kRefineThreads)
             if (L == cntn) lim = cntn - 1;
         }
         const uint32_t cs[2] = {s, s + lim}, ce[2] = {s + lim, e};
+        const uint32_t depth = (nd.z & ~kCovered) + 1;
+        const bool covered = EXACT && (nd.z & kCovered) != 0;
         for (int ch = 0; ch < 2; ++ch) {
             const uint32_t len = ce[ch] - cs[ch];
             bool leaf;
-            if (EXACT) leaf = nd.z + 1 >= nd.w || len == 1;  // KDLineTree.h:37-39
+            if (EXACT) leaf = depth >= nd.w || len == 1;  // KDLineTree.h:37-39
             else leaf = len <= kPiece;
-            const uint4 child = make_uint4(cs[ch], ce[ch], nd.z + 1, nd.w);
+            uint32_t z = depth;
+            if (EXACT && a.coarse) {
+                if (covered) {
+                    z |= kCovered;
+                } else if (len <= kPiece) {  // the first node this small starts a piece
+                    a.flag[cs[ch]] = 1;
+                    z |= kCovered;
+                }
+            }
+            const uint4 child = make_uint4(cs[ch], ce[ch], z, nd.w);
             if (!leaf) {
                 a.next[atomicAdd(a.cnt_next, 1u)] = child;
             } else if (EXACT && len > kPiece) {
                 a.refine[atomicAdd(a.refine_cnt, 1u)] = child;
-            } else {
+            } else if (!(EXACT && a.coarse)) {
                 a.flag[cs[ch]] = 1;
             }
         }
     }
 }
 
-// After the exact phase: Xref/idsnap by permuted position, tag = position.
+// After the exact phase: tag = permuted position (reversed within its cloud
+// for bucket_fps_kdtree), Xref/idsnap indexed by tag.
 template <int D>
 __global__ void build_snapshot(BuildArgs a, float* __restrict__ Xref, uint32_t* __restrict__ idsnap) {
     const uint64_t n = a.n;
     for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n;
          p += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t t = p;
+        if (a.reverse) {  // cloud of p: last c with cloud_off[c] <= p
+            uint32_t lo = 0, hi = a.n_clouds;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) / 2;
+                if (a.cloud_off[mid] <= p) lo = mid;
+                else hi = mid;
+            }
+            t = a.cloud_off[lo] + a.cloud_off[lo + 1] - 1 - p;
+        }
 #pragma unroll
-        for (int d = 0; d < D; ++d) Xref[(uint64_t)d * n + p] = a.X[(uint64_t)d * n + p];
+        for (int d = 0; d < D; ++d) Xref[(uint64_t)d * n + t] = a.X[(uint64_t)d * n + p];
         if (idsnap) {
-            idsnap[p] = a.tag[p];
-            a.tag[p] = (uint32_t)p;
+            idsnap[t] = a.tag[p];
+            a.tag[p] = (uint32_t)t;
         }
     }
 }
@@ -1205,6 +1241,7 @@ struct CloudSet {
     std::vector<uint64_t> off;     // C + 1
     std::vector<uint64_t> height;  // kd-line tree height per cloud
     bool kd = true;
+    bool tie_last = false;         // bucket_fps_kdtree: reversed tags (ties to the last position)
 };
 
 // Device arrays produced by build_clouds.
@@ -1234,6 +1271,16 @@ int build_clouds(const CloudSet& cs, cudaStream_t stream, Scratch& sc, Built& ou
     int rc;
     BuildArgs b{};
     b.n = n;
+    b.coarse = build_only ? 0 : 1;
+    b.reverse = cs.tie_last ? 1 : 0;
+    b.n_clouds = (uint32_t)C;
+    if (cs.tie_last) {
+        uint64_t* d_off;
+        if ((rc = sc.alloc(&d_off, C + 1))) return rc;
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_off, cs.off.data(), (C + 1) * sizeof(uint64_t),
+                                        cudaMemcpyHostToDevice, stream));
+        b.cloud_off = d_off;
+    }
     if ((rc = sc.alloc(&b.X, n * D))) return rc;
     if ((rc = sc.alloc(&b.tag, n))) return rc;
     if ((rc = sc.alloc(&b.sel, n))) return rc;
@@ -1796,6 +1843,7 @@ struct EngineCall {
     float* d_trace;
     cudaStream_t stream;
     int sms;
+    bool tie_last = false;  // bucket_fps_kdtree
     // build-only mode (kd-line): host outputs
     uint64_t* h_perm;
     uint64_t* h_bucket_start;
@@ -1810,6 +1858,7 @@ int run_engine(const EngineCall& c) {
     cs.off = {0, c.n};
     cs.height = {c.height};
     cs.kd = c.kd;
+    cs.tie_last = c.tie_last;
     Built bt;
     int rc;
     if ((rc = build_clouds<D>(cs, c.stream, sc, bt, c.h_perm != nullptr))) return rc;
@@ -1840,8 +1889,10 @@ int run_engine(const EngineCall& c) {
         *c.h_n_buckets = nb;
         return FPSGPU_OK;
     }
-    return sample_grid<D, FMA>(bt, n, c.kd, 0, ~0u, n, c.k, c.h_forced, c.n_forced, 0, c.d_out,
-                               c.d_trace, c.stream, c.sms, sc);
+    // kd-tree: the start's tag is its reversed position
+    const uint64_t f0 = c.tie_last ? n - 1 - c.h_forced[0] : c.h_forced[0];
+    return sample_grid<D, FMA>(bt, n, c.kd, 0, ~0u, n, c.k, c.tie_last ? &f0 : c.h_forced,
+                               c.n_forced, 0, c.d_out, c.d_trace, c.stream, c.sms, sc);
 }
 
 // Many clouds in one go: build all of them together, then one CTA per cloud
@@ -1856,6 +1907,7 @@ struct BatchCall {
     uint64_t* d_out;                  // sum(k), cloud c at out_off[c]
     cudaStream_t stream;
     int sms;
+    bool tie_last = false;            // bucket_fps_kdtree
 };
 
 template <int D, bool FMA>
@@ -1869,6 +1921,7 @@ int run_batch(const BatchCall& bc) {
     cs.off = bc.off;
     cs.height = bc.height;
     cs.kd = bc.kd;
+    cs.tie_last = bc.tie_last;
     Built bt;
     if ((rc = build_clouds<D>(cs, bc.stream, sc, bt, false))) return rc;
 
@@ -1908,8 +1961,9 @@ int run_batch(const BatchCall& bc) {
         out_off[c] = acc;
         acc += bc.k[c];
         // kd-line: the start is a position of the cloud's permuted order, i.e.
-        // a tag; vanilla: the start is an original index, also a tag
-        tag0[c] = bc.off[c] + bc.start[c];
+        // a tag (reversed within the cloud for the kd-tree); vanilla: the
+        // start is an original index, also a tag
+        tag0[c] = bc.off[c] + (bc.tie_last ? bc.off[c + 1] - bc.off[c] - 1 - bc.start[c] : bc.start[c]);
         const uint32_t np = h_cpiece[c + 1] - h_cpiece[c];
         const uint64_t nc = bc.off[c + 1] - bc.off[c];
         if (bc.k[c] == 0) continue;

@@ -133,6 +133,31 @@ Indices bucket_fps_kdline_sampling(FloatRows points, size_t n_samples, size_t he
     return out;
 }
 
+// _bucket_fps_kdtree_sampling (reference src/lib.cpp:467-520)
+Indices bucket_fps_kdtree_sampling(FloatRows points, size_t n_samples, py::object start_obj) {
+    Start start = parse_start(start_obj);
+    if (!start.single) {
+        PyErr_SetString(PyExc_NotImplementedError, "Array of start indices not implemented yet");
+        throw py::error_already_set();
+    }
+    if (points.ndim() != 2) throw py::value_error("points must be a 2D float32 array");
+    const ssize_t P = points.shape(0), C = points.shape(1);
+    if (start.idx >= static_cast<size_t>(P)) throw py::value_error("start_idx out of range");
+    if (n_samples == 0 || n_samples > static_cast<size_t>(P))
+        throw py::value_error("n_samples must be in [1, num_points]");
+    Indices out(n_samples);
+    size_t* out_ptr = static_cast<size_t*>(out.mutable_data());
+    const float* data = points.data();
+    int rc;
+    {
+        py::gil_scoped_release nogil;
+        rc = bucket_fps_kdtree(data, (size_t)P, (size_t)C, n_samples, start.idx, out_ptr);
+    }
+    if (rc != 0)
+        throw std::runtime_error("bucket_fps_kdtree failed with error code " + std::to_string(rc));
+    return out;
+}
+
 // Batched QuickFPS: clouds stored back to back in `points` (rows
 // [offsets[c], offsets[c+1]) form cloud c).  Returns one uint64 array with the
 // clouds' local indices back to back (cloud c at sum(n_samples[:c])).
@@ -173,8 +198,8 @@ Indices bucket_fps_kdline_sampling_batch(FloatRows points, Indices offsets, Indi
 [[noreturn]] void not_in_gpu_build(const char* name) {
     PyErr_SetString(PyExc_NotImplementedError,
                     (std::string(name) +
-                     " is not part of the GB300 build; it provides fps_sampling and "
-                     "bucket_fps_kdline_sampling")
+                     " is not part of the GB300 build; it provides fps_sampling, "
+                     "bucket_fps_kdline_sampling and bucket_fps_kdtree_sampling")
                         .c_str());
     throw py::error_already_set();
 }
@@ -253,8 +278,15 @@ PYBIND11_MODULE(_fpsample, m) {
     m.def("_fps_npdu_sampling", [](py::args, py::kwargs) { not_in_gpu_build("_fps_npdu_sampling"); });
     m.def("_fps_npdu_kdtree_sampling",
           [](py::args, py::kwargs) { not_in_gpu_build("_fps_npdu_kdtree_sampling"); });
-    m.def("_bucket_fps_kdtree_sampling",
-          [](py::args, py::kwargs) { not_in_gpu_build("_bucket_fps_kdtree_sampling"); });
+    m.def("_bucket_fps_kdtree_sampling", &bucket_fps_kdtree_sampling, R"pbdoc(
+            Bucket FPS sampling with a full kd-tree (QuickFPS) on the GPU
+            Args:
+                points (np.ndarray[float32, 2D]): N x C point array, C <= 8.
+                n_samples (int): number of samples to pick.
+                start_idx (int): first index (a position of the tree's permuted order).
+            Returns:
+                np.ndarray[uint64]: sampled point indices.
+    )pbdoc");
 
     m.def("_bucket_fps_kdline_sampling_batch", &bucket_fps_kdline_sampling_batch,
           "many clouds in one GPU call: (points, offsets, n_samples, heights, starts) -> indices");

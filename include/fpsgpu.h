@@ -54,6 +54,19 @@ int bucket_fps_kdline(const float *raw_data, size_t n_points, size_t dim,
                       size_t *sampled_point_indices);
 
 /*
+ * Replaces the reference's C ABI of the same name and signature
+ * (src/wrapper.hpp:102-116, kdtree_sample :29-43): QuickFPS on a full kd-tree
+ * (split until every leaf holds one point, KDTree.h:26).  Same start rule and
+ * return codes as bucket_fps_kdline.  Subtree maxima are combined with
+ * KDNode::updateMaxPoint (KDNode.h:41-46), which keeps the left child only when
+ * it is strictly farther, so among equal distances the LAST position of the
+ * tree's order wins (bucket_fps_kdline: the first).
+ */
+int bucket_fps_kdtree(const float *raw_data, size_t n_points, size_t dim,
+                      size_t n_samples, size_t start_idx,
+                      size_t *sampled_point_indices);
+
+/*
  * Vanilla FPS with one or more start indices.  The reference has no C ABI for
  * this path; this is the C form of _fps_sampling (src/lib.cpp:249-270), which
  * dispatches to fps_sampling (lib.cpp:188-246, n_start == 1) and
@@ -77,6 +90,11 @@ int fpsgpu_fps(const float *raw_data, size_t n_points, size_t dim,
 int fpsgpu_kdline_device(const float *d_points, size_t n_points, size_t dim,
                          size_t n_samples, size_t start_idx, size_t height,
                          uint64_t *d_out, float *d_trace, void *stream);
+
+/* bucket_fps_kdtree on device buffers; d_trace as in fpsgpu_kdline_device. */
+int fpsgpu_kdtree_device(const float *d_points, size_t n_points, size_t dim,
+                         size_t n_samples, size_t start_idx, uint64_t *d_out,
+                         float *d_trace, void *stream);
 
 int fpsgpu_fps_device(const float *d_points, size_t n_points, size_t dim,
                       size_t n_samples, const size_t *h_start, size_t n_start,

@@ -438,3 +438,54 @@ done:
     free(perm); free(bstart); free(w); free(dis);
     return rc;
 }
+
+/* bucket_fps_kdtree (wrapper.hpp:29-43, KDTree.h:13-51, KDNode.h:41-46 and
+ * :105-166): the same build with no height limit (KDTree::leftNode: a node is a
+ * leaf when it holds one point), started at permuted position start_idx, and
+ * FPS in which subtree maxima are combined by KDNode::updateMaxPoint, which
+ * keeps the left child only when it is strictly farther.  Among equal running
+ * distances the LAST position of the tree's order therefore wins; the
+ * deferred-reference scheme never changes a value (as for kd-line).  Checked
+ * against the reference's own output (tests/golden), including integer grids
+ * full of ties. */
+int oracle_kdtree(const float *pts, size_t n, size_t dim, size_t k, size_t start_idx,
+                  int fma_mode, uint64_t *out) {
+    if (dim == 0 || dim > 8) return ORACLE_BAD_DIM;
+    if (start_idx >= n) return ORACLE_BAD_START;
+    uint64_t *perm = (uint64_t *)malloc(n * sizeof(uint64_t));
+    uint64_t *bstart = (uint64_t *)malloc(n * sizeof(uint64_t));
+    float *w = (float *)malloc(n * dim * sizeof(float));
+    float *dis = (float *)malloc(n * sizeof(float));
+    int rc = ORACLE_OK;
+    if (!perm || !bstart || !w || !dis) {
+        rc = ORACLE_NO_MEMORY;
+        goto done;
+    }
+    size_t nb;
+    rc = oracle_kdline_build(pts, n, dim, (size_t)-1, perm, bstart, &nb);
+    if (rc) goto done;
+    for (size_t p = 0; p < n; ++p) {
+        memcpy(w + p * dim, pts + (size_t)perm[p] * dim, dim * sizeof(float));
+        dis[p] = FLT_MAX;
+    }
+    size_t cur = start_idx;
+    for (size_t t = 0; t < k; ++t) {
+        out[t] = perm[cur];
+        if (t + 1 == k) break;
+        const float *r = w + cur * dim;
+        float best = -FLT_MAX;
+        size_t pick = 0;
+        for (size_t p = 0; p < n; ++p) {
+            float d = sqdist(w + p * dim, r, dim, fma_mode);
+            if (d < dis[p]) dis[p] = d;
+            if (dis[p] >= best) {  /* updateMaxPoint: ties go right */
+                best = dis[p];
+                pick = p;
+            }
+        }
+        cur = pick;
+    }
+done:
+    free(perm); free(bstart); free(w); free(dis);
+    return rc;
+}

@@ -60,8 +60,10 @@ class Oracle:
         lib.oracle_fps.argtypes = [_f32p, _sz, _sz, _sz, _u64p, _sz, ctypes.c_int, _u64p, _f32p]
         lib.oracle_kdline.argtypes = [_f32p, _sz, _sz, _sz, _sz, _sz, ctypes.c_int, _u64p, _f32p, _u64p]
         lib.oracle_kdline_direct.argtypes = [_f32p, _sz, _sz, _sz, _sz, _sz, ctypes.c_int, _u64p]
+        lib.oracle_kdtree.argtypes = [_f32p, _sz, _sz, _sz, _sz, ctypes.c_int, _u64p]
         lib.oracle_kdline_build.argtypes = [_f32p, _sz, _sz, _sz, _u64p, _u64p, ctypes.POINTER(_sz)]
-        for f in ("oracle_fps", "oracle_kdline", "oracle_kdline_direct", "oracle_kdline_build"):
+        for f in ("oracle_fps", "oracle_kdline", "oracle_kdline_direct", "oracle_kdline_build",
+                  "oracle_kdtree"):
             getattr(lib, f).restype = ctypes.c_int
         self.lib = lib
 
@@ -110,6 +112,16 @@ class Oracle:
                                            FP_MODES[fp_mode], _ptr(out, _u64p))
         if rc:
             raise RuntimeError(f"oracle_kdline_direct failed with code {rc}")
+        return out
+
+    def kdtree(self, pc, k, start, fp_mode="nofma"):
+        """bucket_fps_kdtree: unbounded-height build, ties to the last position."""
+        pc = self._pts(pc)
+        out = np.zeros(k, np.uint64)
+        rc = self.lib.oracle_kdtree(_ptr(pc, _f32p), pc.shape[0], pc.shape[1], k, start,
+                                    FP_MODES[fp_mode], _ptr(out, _u64p))
+        if rc:
+            raise RuntimeError(f"oracle_kdtree failed with code {rc}")
         return out
 
     def kdline_build(self, pc, h):

@@ -91,3 +91,18 @@ CASES.append(_c("tiny_kdline_h1", "kdline", "uniform", {"n": 2, "d": 3, "seed": 
 CASES.append(_c("one_fps", "fps", "uniform", {"n": 1, "d": 4, "seed": 52}, 1, 0))
 # Gaussian mixture where the FMA and non-FMA builds diverge (at sample 3912)
 CASES.append(_c("gmm128k_kdline_h7", "kdline", "gmm", {"n": 131072, "seed": 1}, 8192, 0, 7))
+# bucket_fps_kdtree (unbounded-height tree, ties to the last position):
+# continuous data, every dimension, integer grids and repeated points
+CASES.append(_c("u4k_kdtree", "kdtree", "uniform", U4, 1024, 0))
+CASES.append(_c("bench42_kdtree", "kdtree", "bench42", B, 1024, 0))
+for d in range(1, 9):
+    CASES.append(_c(f"d{d}_kdtree_s777", "kdtree", "uniform",
+                    {"n": 1500, "d": d, "seed": 10 + d}, 300, 777))
+for d in (1, 2, 3, 5):
+    CASES.append(_c(f"grid{d}_kdtree", "kdtree", "grid",
+                    {"n": 3000, "d": d, "levels": 4, "seed": 30 + d}, 300, 7, stored=True))
+CASES.append(_c("grid_small_kdtree_all", "kdtree", "grid", gs, 200, 3, stored=True))
+CASES.append(_c("dups_kdtree", "kdtree", "dups", dp, 512, 0, stored=True))
+CASES.append(_c("equal_kdtree", "kdtree", "equal", eq, 64, 10))
+CASES.append(_c("tiny_kdtree", "kdtree", "uniform", {"n": 2, "d": 3, "seed": 51}, 2, 1))
+CASES.append(_c("one_kdtree", "kdtree", "uniform", {"n": 1, "d": 4, "seed": 52}, 1, 0))

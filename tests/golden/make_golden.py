@@ -6,7 +6,8 @@ Run where the reference sources are mounted (they are not on the GPU hosts):
     python tests/golden/make_golden.py
 
 Every expected output comes from the reference's public Python API
-(``fpsample.fps_sampling`` / ``fpsample.bucket_fps_kdline_sampling``), run
+(``fpsample.fps_sampling`` / ``bucket_fps_kdline_sampling`` /
+``bucket_fps_kdtree_sampling``), run
 through its two builds: "nofma" (default x86-64 code, no contraction) and
 "fma" (same source with FMA contraction enabled).  Inputs that a seeded
 generator reproduces are stored as (generator, sha256) and regenerated by the
@@ -46,6 +47,8 @@ def main() -> None:
         for mode, ref in refs.items():
             if case["op"] == "fps":
                 out = ref.fps_sampling(pts, case["k"], case["start"])
+            elif case["op"] == "kdtree":
+                out = ref.bucket_fps_kdtree_sampling(pts, case["k"], case["start"])
             else:
                 out = ref.bucket_fps_kdline_sampling(pts, case["k"], case["h"], case["start"])
             arrays[f"{case['name']}__{mode}"] = np.asarray(out, dtype=np.uint64)

@@ -69,10 +69,28 @@ def test_extension_errors_match_reference():
 
 
 def test_out_of_scope_variants_raise():
-    for f in (lambda: fps.fps_npdu_sampling(PC, 4), lambda: fps.fps_npdu_kdtree_sampling(PC, 4),
-              lambda: fps.bucket_fps_kdtree_sampling(PC, 4)):
+    for f in (lambda: fps.fps_npdu_sampling(PC, 4), lambda: fps.fps_npdu_kdtree_sampling(PC, 4)):
         with pytest.raises(NotImplementedError):
             f()
+
+
+def test_kdtree_argument_checks_match_reference():
+    # reference src/fpsample/__init__.py:159-171 and src/lib.cpp:467-520
+    with pytest.raises(AssertionError, match="n_samples should be >= 1"):
+        fps.bucket_fps_kdtree_sampling(PC, 0)
+    with pytest.raises(AssertionError, match="n_pts should be >= n_samples"):
+        fps.bucket_fps_kdtree_sampling(PC, PC.shape[0] + 1)
+    with pytest.raises(AssertionError, match="start_idx should be None"):
+        fps.bucket_fps_kdtree_sampling(PC, 3, PC.shape[0])
+    pc = np.zeros((5, 3), np.float32)
+    with pytest.raises(NotImplementedError, match="Array of start indices"):
+        _fpsample._bucket_fps_kdtree_sampling(pc, 3, np.array([0, 1], np.uint64))
+    with pytest.raises(ValueError, match="start_idx out of range"):
+        _fpsample._bucket_fps_kdtree_sampling(pc, 3, 10)
+    with pytest.raises(ValueError, match=r"n_samples must be in \[1, num_points\]"):
+        _fpsample._bucket_fps_kdtree_sampling(pc, 0, 0)
+    with pytest.raises(TypeError):
+        _fpsample._bucket_fps_kdtree_sampling(pc, 3, "0")
 
 
 def test_exports_and_version():

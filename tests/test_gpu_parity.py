@@ -36,6 +36,8 @@ def _api(case):
     if case["op"] == "fps":
         st = case["start"]
         return fps.fps_sampling(pts, case["k"], st)
+    if case["op"] == "kdtree":
+        return fps.bucket_fps_kdtree_sampling(pts, case["k"], case["start"])
     return fps.bucket_fps_kdline_sampling(pts, case["k"], case["h"], case["start"])
 
 
@@ -43,6 +45,8 @@ def _cabi(case):
     pts = case["points"]
     if case["op"] == "fps":
         return capi.fps(pts, case["k"], case["start"])
+    if case["op"] == "kdtree":
+        return capi.bucket_fps_kdtree(pts, case["k"], case["start"])
     return capi.bucket_fps_kdline(pts, case["k"], case["start"], case["h"])
 
 
@@ -53,7 +57,10 @@ def test_golden_python_api(case, mode):
     np.testing.assert_array_equal(got, case["expected"][mode])
 
 
-@pytest.mark.parametrize("case", CASES[::3], ids=[c["name"] for c in CASES[::3]])
+ABI_CASES = CASES[::3] + [c for c in CASES if c["op"] == "kdtree"][1::3]
+
+
+@pytest.mark.parametrize("case", ABI_CASES, ids=[c["name"] for c in ABI_CASES])
 def test_golden_c_abi(case, mode):
     np.testing.assert_array_equal(_cabi(case), case["expected"][mode])
 
@@ -81,6 +88,27 @@ def test_random_vs_oracle(seed, mode):
     np.testing.assert_array_equal(fps.fps_sampling(pts, k, s), ORACLE.fps(pts, k, s, mode))
     np.testing.assert_array_equal(fps.bucket_fps_kdline_sampling(pts, k, h, s),
                                   ORACLE.kdline(pts, k, h, s, mode))
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_kdtree_random_vs_oracle(seed, mode):
+    pts, k, s, _ = _random_case(seed)
+    if pts.shape[1] > 8:
+        pts = pts[:, :8]
+    np.testing.assert_array_equal(fps.bucket_fps_kdtree_sampling(pts, k, s),
+                                  ORACLE.kdtree(pts, k, s, mode))
+
+
+def test_kdtree_large_cloud_and_trace(mode):
+    """300K points: the kd-tree build reaches ~20 exact levels; plain calls run
+    on a cluster, traced calls on the grid sampler."""
+    torch = pytest.importorskip("torch")
+    pts = W.gmm_cloud(300_000, seed=12)
+    want = ORACLE.kdtree(pts, 2000, 17, mode)
+    np.testing.assert_array_equal(fps.bucket_fps_kdtree_sampling(pts, 2000, 17), want)
+    out, tr = capi.kdtree_tensor(torch.from_numpy(pts).cuda(), 2000, 17, trace=True)
+    np.testing.assert_array_equal(out.cpu().numpy().astype(np.uint64), want)
+    assert np.all(np.diff(tr.cpu().numpy()[1:]) <= 0)
 
 
 @pytest.mark.parametrize("seed", range(6))

@@ -21,9 +21,19 @@ def test_oracle_matches_reference(case, mode):
     pts = case["points"]
     if case["op"] == "fps":
         got = ORACLE.fps(pts, case["k"], case["start"], mode)
+    elif case["op"] == "kdtree":
+        got = ORACLE.kdtree(pts, case["k"], case["start"], mode)
     else:
         got = ORACLE.kdline(pts, case["k"], case["h"], case["start"], mode)
     np.testing.assert_array_equal(got, case["expected"][mode])
+
+
+def test_kdtree_cases_contain_ties_that_separate_it_from_kdline():
+    # on tie-heavy grids the kd-tree (ties to the last position) and an
+    # unbounded kd-line (ties to the first) disagree, so the tie rule is pinned
+    c = next(c for c in CASES if c["name"] == "grid2_kdtree")
+    line = ORACLE.kdline(c["points"], c["k"], 64, c["start"], "nofma")
+    assert not np.array_equal(line, c["expected"]["nofma"])
 
 
 def test_fma_builds_really_differ():
