@@ -39,7 +39,11 @@ try:
         _fps_sampling,
         _get_fp_mode,
         _kdline_build,
+        _sample_points,
         _set_fp_mode,
+        ALGO_FPS,
+        ALGO_KDLINE,
+        ALGO_KDTREE,
     )
 except ImportError as e:  # loud: no CPU fallback exists
     raise ImportError(
@@ -202,6 +206,63 @@ def bucket_fps_kdtree_sampling(
     return _bucket_fps_kdtree_sampling(pc, n_samples, start_idx)
 
 
+def _starts_array(start_idx) -> np.ndarray:
+    return np.atleast_1d(np.asarray(start_idx, dtype=np.uint64))
+
+
+def fps_sampling_points(pc: np.ndarray, n_samples: int,
+                        start_idx: Optional[Union[int, List[int]]] = None):
+    """fps_sampling plus the gather the caller would do next: returns
+    (indices, pc[indices]) with the points as float32 [n_samples, D], written by
+    the sampler as it picks them (no second pass over the cloud).  Same
+    checks and indices as fps_sampling."""
+    assert n_samples >= 1, "n_samples should be >= 1"
+    assert pc.ndim == 2
+    n_pts, _ = pc.shape
+    assert n_pts >= n_samples, "n_pts should be >= n_samples"
+    if isinstance(start_idx, int):
+        assert 0 <= start_idx < n_pts, "start_idx should be None or 0 <= start_idx < n_pts"
+    if isinstance(start_idx, list):
+        assert len(start_idx) <= n_samples, "len(start_idx) should be <= n_samples"
+        for idx in start_idx:
+            assert 0 <= idx < n_pts, "start_idx should be None or 0 <= start_idx < n_pts"
+    pc = np.ascontiguousarray(pc, dtype=np.float32)
+    start_idx = get_start_idx(n_pts, start_idx)
+    return _sample_points(ALGO_FPS, pc, n_samples, _starts_array(start_idx), 0)
+
+
+def bucket_fps_kdline_sampling_points(pc: np.ndarray, n_samples: int, h: int,
+                                      start_idx: Optional[int] = None):
+    """bucket_fps_kdline_sampling plus the fused gather: (indices, points)."""
+    assert n_samples >= 1, "n_samples should be >= 1"
+    assert pc.ndim == 2
+    n_pts, _ = pc.shape
+    assert n_pts >= n_samples, "n_pts should be >= n_samples"
+    assert h >= 1, "h should be >= 1"
+    assert 2**h <= n_pts, "2**h should be <= n_pts"
+    assert (
+        start_idx is None or 0 <= start_idx < n_pts
+    ), "start_idx should be None or 0 <= start_idx < n_pts"
+    pc = np.ascontiguousarray(pc, dtype=np.float32)
+    start_idx = get_start_idx(n_pts, start_idx)
+    return _sample_points(ALGO_KDLINE, pc, n_samples, _starts_array(start_idx), h)
+
+
+def bucket_fps_kdtree_sampling_points(pc: np.ndarray, n_samples: int,
+                                      start_idx: Optional[int] = None):
+    """bucket_fps_kdtree_sampling plus the fused gather: (indices, points)."""
+    assert n_samples >= 1, "n_samples should be >= 1"
+    assert pc.ndim == 2
+    n_pts, _ = pc.shape
+    assert n_pts >= n_samples, "n_pts should be >= n_samples"
+    assert (
+        start_idx is None or 0 <= start_idx < n_pts
+    ), "start_idx should be None or 0 <= start_idx < n_pts"
+    pc = np.ascontiguousarray(pc, dtype=np.float32)
+    start_idx = get_start_idx(n_pts, start_idx)
+    return _sample_points(ALGO_KDTREE, pc, n_samples, _starts_array(start_idx), 0)
+
+
 def set_fp_mode(mode: str) -> None:
     """Select the distance arithmetic to match: "nofma" (reference built without
     FMA contraction, the x86-64 default) or "fma" (contracting build)."""
@@ -229,6 +290,9 @@ __all__ = [
     "fps_npdu_sampling",
     "fps_npdu_kdtree_sampling",
     "bucket_fps_kdtree_sampling",
+    "fps_sampling_points",
+    "bucket_fps_kdline_sampling_points",
+    "bucket_fps_kdtree_sampling_points",
     "bucket_fps_kdline_sampling",
     "bucket_fps_kdline_sampling_batch",
     "set_fp_mode",

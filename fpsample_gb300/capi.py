@@ -44,6 +44,12 @@ SIGNATURES = {
     "fpsgpu_stats_timing": (None, [ctypes.c_int]),
     "fpsgpu_last_error": (ctypes.c_char_p, []),
     "fpsgpu_measure_bandwidth": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "fpsgpu_sample_points": (ctypes.c_int, [ctypes.c_int, _f32p, _sz, _sz, _sz, _szp, _sz, _sz,
+                                            _szp, _f32p]),
+    "fpsgpu_sample_points_device": (ctypes.c_int, [ctypes.c_int, _vp, _sz, _sz, _sz, _szp, _sz,
+                                                   _sz, _vp, _vp, _vp]),
+    "fpsgpu_kdline_batch_points_device": (ctypes.c_int, [_vp, _szp, _sz, _sz, _szp, _szp, _szp,
+                                                         _vp, _vp, _vp]),
     "fpsgpu_version": (ctypes.c_char_p, []),
 }
 
@@ -320,3 +326,31 @@ def measure_bandwidth(level: int) -> float:
     v = ctypes.c_double(0.0)
     _check("fpsgpu_measure_bandwidth", lib().fpsgpu_measure_bandwidth(level, ctypes.byref(v)))
     return v.value
+
+
+ALGO_FPS, ALGO_KDLINE, ALGO_KDTREE = 0, 1, 2
+
+
+def sample_points(algo: int, pc, n_samples: int, starts, height: int = 0):
+    """fpsgpu_sample_points, host buffers: (uint64 indices, float32 [K, D] points)."""
+    a = _rows(pc)
+    st = np.atleast_1d(np.asarray(starts, dtype=np.uint64))
+    out = np.zeros(n_samples, np.uint64)
+    xyz = np.zeros((n_samples, a.shape[1]), np.float32)
+    _check("fpsgpu_sample_points",
+           lib().fpsgpu_sample_points(algo, a.ctypes.data_as(_f32p), a.shape[0], a.shape[1],
+                                      n_samples, st.ctypes.data_as(_szp), st.size, height,
+                                      out.ctypes.data_as(_szp), xyz.ctypes.data_as(_f32p)))
+    return out, xyz
+
+
+def kdline_batch_points_device(points_ptr: int, offsets, dim: int, n_samples, heights, starts,
+                               out_ptr: int, out_points_ptr: int, stream=0) -> None:
+    off = np.asarray(offsets, dtype=np.uint64)
+    ks = np.asarray(n_samples, dtype=np.uint64)
+    hs = np.asarray(heights, dtype=np.uint64)
+    ss = np.asarray(starts, dtype=np.uint64)
+    _check("fpsgpu_kdline_batch_points_device",
+           lib().fpsgpu_kdline_batch_points_device(
+               points_ptr, off.ctypes.data_as(_szp), len(ks), dim, ks.ctypes.data_as(_szp),
+               ss.ctypes.data_as(_szp), hs.ctypes.data_as(_szp), out_ptr, out_points_ptr, stream))

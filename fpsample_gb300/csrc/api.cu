@@ -385,9 +385,10 @@ int resolve_stream(void* stream, DevCtx* ctx, cudaStream_t* out) {
 // multi-CTA sampler run_engine uses.  Results are identical either way.
 int single_via_batch(const float* d_points, size_t n, size_t dim, size_t k, size_t start,
                      size_t height, bool kd, uint64_t* d_out, cudaStream_t stream, int sms,
-                     bool tie_last = false) {
+                     bool tie_last = false, float* d_out_pts = nullptr) {
     BatchCall b;
     b.tie_last = tie_last;
+    b.d_out_pts = d_out_pts;
     b.d_points = d_points;
     b.off = {0, (uint64_t)n};
     b.k = {(uint64_t)k};
@@ -401,8 +402,10 @@ int single_via_batch(const float* d_points, size_t n, size_t dim, size_t k, size
 }
 
 int fps_device_impl(const float* d_points, size_t n, size_t dim, size_t k, const size_t* h_start,
-                    size_t n_start, uint64_t* d_out, float* d_trace, cudaStream_t stream, int sms) {
+                    size_t n_start, uint64_t* d_out, float* d_trace, cudaStream_t stream, int sms,
+                    float* d_out_pts = nullptr) {
     VanillaCall c{};
+    c.d_out_pts = d_out_pts;
     c.d_points = d_points;
     c.n = n;
     c.dim = (int)dim;
@@ -415,8 +418,10 @@ int fps_device_impl(const float* d_points, size_t n, size_t dim, size_t k, const
     c.sms = sms;
     if (dim <= 8 && n > kVanillaBruteMax) {
         if (n_start == 1 && d_trace == nullptr)
-            return single_via_batch(d_points, n, dim, k, h_start[0], 0, false, d_out, stream, sms);
+            return single_via_batch(d_points, n, dim, k, h_start[0], 0, false, d_out, stream, sms,
+                                    false, d_out_pts);
         EngineCall e{};
+        e.d_out_pts = d_out_pts;
         e.d_points = d_points;
         e.n = n;
         e.k = k;
@@ -458,13 +463,14 @@ int check_kdline_args(size_t n, size_t dim, size_t start) {
 // to the last position of the tree's order.
 int kdline_device_impl(const float* d_points, size_t n, size_t dim, size_t k, size_t start,
                        size_t height, uint64_t* d_out, float* d_trace, cudaStream_t stream, int sms,
-                       bool tie_last = false) {
+                       bool tie_last = false, float* d_out_pts = nullptr) {
     if (d_trace == nullptr)
         return single_via_batch(d_points, n, dim, k, start, height, true, d_out, stream, sms,
-                                tie_last);
+                                tie_last, d_out_pts);
     const uint64_t forced = start;
     EngineCall c{};
     c.tie_last = tie_last;
+    c.d_out_pts = d_out_pts;
     c.d_points = d_points;
     c.n = n;
     c.k = k;
@@ -627,7 +633,72 @@ int fpsgpu_kdline_batch_device(const float* d_points, const size_t* h_offsets, s
                                size_t dim, const size_t* h_n_samples, const size_t* h_start_idx,
                                const size_t* h_height, uint64_t* d_out, void* stream) {
     return fpsgpu::kdline_batch_device_capped(d_points, h_offsets, n_clouds, dim, h_n_samples,
-                                              h_start_idx, h_height, d_out, stream, 0);
+                                              h_start_idx, h_height, d_out, stream, 0, nullptr);
+}
+
+int fpsgpu_kdline_batch_points_device(const float* d_points, const size_t* h_offsets,
+                                      size_t n_clouds, size_t dim, const size_t* h_n_samples,
+                                      const size_t* h_start_idx, const size_t* h_height,
+                                      uint64_t* d_out, float* d_out_points, void* stream) {
+    return fpsgpu::kdline_batch_device_capped(d_points, h_offsets, n_clouds, dim, h_n_samples,
+                                              h_start_idx, h_height, d_out, stream, 0, d_out_points);
+}
+
+int fpsgpu_sample_points_device(int algo, const float* d_points, size_t n_points, size_t dim,
+                                size_t n_samples, const size_t* h_start, size_t n_start,
+                                size_t height, uint64_t* d_out, float* d_out_points, void* stream) {
+    clear_error();
+    int rc;
+    if (algo == FPSGPU_ALGO_FPS) {
+        if ((rc = check_fps_args(n_points, dim, n_samples, h_start, n_start))) return rc;
+    } else if (algo == FPSGPU_ALGO_KDLINE || algo == FPSGPU_ALGO_KDTREE) {
+        if (!h_start || n_start != 1)
+            return set_error(FPSGPU_ERR_ARG, "kd-line and kd-tree take exactly one start index");
+        if ((rc = check_kdline_args(n_points, dim, h_start[0]))) return rc;
+    } else {
+        return set_error(FPSGPU_ERR_ARG, "unknown algorithm %d", algo);
+    }
+    if (n_samples == 0) return FPSGPU_OK;
+    DevCtx ctx;
+    cudaStream_t s;
+    if ((rc = resolve_stream(stream, &ctx, &s))) return rc;
+    if (algo == FPSGPU_ALGO_FPS)
+        return fps_device_impl(d_points, n_points, dim, n_samples, h_start, n_start, d_out, nullptr,
+                               s, ctx.sms, d_out_points);
+    const bool tree = algo == FPSGPU_ALGO_KDTREE;
+    return kdline_device_impl(d_points, n_points, dim, n_samples, h_start[0],
+                              tree ? ~(size_t)0 : height, d_out, nullptr, s, ctx.sms, tree,
+                              d_out_points);
+}
+
+int fpsgpu_sample_points(int algo, const float* raw_data, size_t n_points, size_t dim,
+                         size_t n_samples, const size_t* start_idx, size_t n_start, size_t height,
+                         size_t* sampled_point_indices, float* sampled_points) {
+    clear_error();
+    if (n_samples == 0) return FPSGPU_OK;
+    if (!raw_data || !sampled_point_indices) return set_error(FPSGPU_ERR_ARG, "null argument");
+    DevCtx ctx;
+    int rc;
+    if ((rc = current_ctx(&ctx))) return rc;
+    Scratch sc(ctx.stream);
+    float* d_pts;
+    uint64_t* d_out;
+    float* d_xyz = nullptr;
+    if ((rc = sc.alloc(&d_pts, n_points * (dim ? dim : 1)))) return rc;
+    if ((rc = sc.alloc(&d_out, n_samples))) return rc;
+    if (sampled_points && (rc = sc.alloc(&d_xyz, n_samples * (dim ? dim : 1)))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_pts, raw_data, n_points * dim * sizeof(float),
+                                    cudaMemcpyHostToDevice, ctx.stream));
+    if ((rc = fpsgpu_sample_points_device(algo, d_pts, n_points, dim, n_samples, start_idx, n_start,
+                                          height, d_out, d_xyz, ctx.stream)))
+        return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(sampled_point_indices, d_out, n_samples * sizeof(uint64_t),
+                                    cudaMemcpyDeviceToHost, ctx.stream));
+    if (sampled_points)
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(sampled_points, d_xyz, n_samples * dim * sizeof(float),
+                                        cudaMemcpyDeviceToHost, ctx.stream));
+    FPSGPU_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
+    return FPSGPU_OK;
 }
 
 }  // extern "C"
@@ -636,7 +707,7 @@ namespace fpsgpu {
 int kdline_batch_device_capped(const float* d_points, const size_t* h_offsets, size_t n_clouds,
                                size_t dim, const size_t* h_n_samples, const size_t* h_start_idx,
                                const size_t* h_height, uint64_t* d_out, void* stream,
-                               int max_grid) {
+                               int max_grid, float* d_out_pts) {
     clear_error();
     if (n_clouds == 0) return FPSGPU_OK;
     if (!h_offsets || !h_n_samples || !h_start_idx || !h_height)
@@ -665,6 +736,7 @@ int kdline_batch_device_capped(const float* d_points, const size_t* h_offsets, s
     b.height.assign(h_height, h_height + n_clouds);
     b.kd = true;
     b.d_out = d_out;
+    b.d_out_pts = d_out_pts;
     b.stream = s;
     b.sms = max_grid > 0 && max_grid < ctx.sms ? max_grid : ctx.sms;
     return fp_mode() == FPSGPU_FP_FMA ? run_batch_fma((int)dim, b) : run_batch_nofma((int)dim, b);

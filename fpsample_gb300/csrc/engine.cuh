@@ -518,6 +518,7 @@ struct SampleArgs {
     uint32_t n_forced;
     uint64_t* out;
     float* trace;
+    float* out_pts;          // null, or [k][D]: coordinates of every sample (fused gather)
     uint64_t* slots;
     int* err;
     unsigned long long* counters;  // [2]: boxes tested, distances recomputed
@@ -605,7 +606,10 @@ __global__ void __launch_bounds__(kSampleThreads, 1) fps_sample(SampleArgs a) {
     const uint32_t q1 = q0 + pw < np ? q0 + pw : np;
 
     const uint32_t tag0 = (uint32_t)a.forced[0];
-    if (tid < D) s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
+    if (tid < D) {
+        s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
+        if (blockIdx.x == 0 && a.out_pts && a.k > 0) a.out_pts[tid] = s_ref[tid];
+    }
     if (tid == 0) s_abort = 0;
     if (blockIdx.x == 0 && tid == 0 && a.k > 0) {
         a.out[0] = KD ? tag0 : tag0 - a.id_offset;
@@ -648,7 +652,11 @@ __global__ void __launch_bounds__(kSampleThreads, 1) fps_sample(SampleArgs a) {
             if (!ok) {
                 if (lane == 0) s_abort = 1;
             } else {
-                if (lane < D) s_ref[lane] = a.Xref[(uint64_t)lane * n + tg];
+                if (lane < D) {
+                    const float v = a.Xref[(uint64_t)lane * n + tg];
+                    s_ref[lane] = v;
+                    if (blockIdx.x == 0 && a.out_pts) a.out_pts[(t + 1) * D + lane] = v;
+                }
                 if (blockIdx.x == 0 && lane == 0) {
                     a.out[t + 1] = KD ? tg : tg - a.id_offset;
                     if (a.trace) a.trace[t + 1] = forced ? INFINITY : key_dist(g);
@@ -828,6 +836,7 @@ struct BatchArgs {
     uint32_t cap;               // pieces per cloud at most (batch_slots(D) x threads)
     uint32_t mcap;              // points that fit in shared memory
     int* err;
+    float* out_pts;             // null, or [sum k][D]: coordinates of every sample (fused gather)
 };
 
 inline size_t batch_smem_bytes(int D, uint32_t cap, uint32_t mcap) {
@@ -930,6 +939,11 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
         for (int d = 0; d < D; ++d) r[d] = a.Xref[(uint64_t)d * n + tag0];
         // outputs hold tags while sampling (kd-line tags are mapped at the end)
         if (rank == 0 && tid == 0 && K > 0) a.out[ooff] = KD ? tag0 : tag0 - coff;
+        if (rank == 0 && a.out_pts && K > 0) {
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+                if (tid == d) a.out_pts[ooff * D + d] = r[d];
+        }
         if (tid < 3) s_best[tid] = 0ull;
         __syncthreads();
 
@@ -1028,6 +1042,11 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
                 }
                 s_best[par == 0 ? 2 : par - 1] = 0ull;  // last sample's slot: everyone has read it
             }
+            if (rank == 0 && a.out_pts) {  // the winner's coordinates are the new r
+#pragma unroll
+                for (int d = 0; d < D; ++d)
+                    if (tid == 32 + d) a.out_pts[(ooff + t + 1) * D + d] = r[d];
+            }
             par = par == 2 ? 0 : par + 1;
         }
         __syncthreads();  // thread 0's output writes are visible to the CTA
@@ -1108,7 +1127,10 @@ __global__ void __launch_bounds__(kRegThreads, 1) grid_sample_reg(SampleArgs a) 
         s_pe[i] = a.pstart[q + 1];
     }
     const uint32_t tag0 = (uint32_t)a.forced[0];
-    if (tid < D) s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
+    if (tid < D) {
+        s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
+        if (blockIdx.x == 0 && a.out_pts && a.k > 0) a.out_pts[tid] = s_ref[tid];
+    }
     if (tid == 0) s_abort = 0;
     // outputs hold tags while sampling; kd-line tags are mapped afterwards
     if (rank == 0 && tid == 0 && a.k > 0) {
@@ -1209,8 +1231,12 @@ __global__ void __launch_bounds__(kRegThreads, 1) grid_sample_reg(SampleArgs a) 
                 if (lane == 0) s_abort = 1;
             } else {
 #pragma unroll
-                for (int d = 0; d < D; ++d)
-                    if (lane == d) s_ref[d] = wc[d];  // static indices keep wc in registers
+                for (int d = 0; d < D; ++d) {
+                    if (lane == d) {  // static indices keep wc in registers
+                        s_ref[d] = wc[d];
+                        if (blockIdx.x == 0 && a.out_pts) a.out_pts[(t + 1) * D + d] = wc[d];
+                    }
+                }
                 if (rank == 0 && lane == 0) {
                     a.out[t + 1] = KD ? tg : tg - a.id_offset;
                     if (a.trace) a.trace[t + 1] = forced ? INFINITY : key_dist(g);
@@ -1447,6 +1473,7 @@ struct GridSmemArgs {
     uint64_t id_offset;
     uint64_t* out;
     float* trace;
+    float* out_pts;  // null, or [k][D] (fused gather)
     uint64_t* slots;
     int* err;
     unsigned long long* counters;
@@ -1498,7 +1525,10 @@ __global__ void __launch_bounds__(kSmemThreads, 1) grid_sample_smem(GridSmemArgs
         }
     }
     const uint32_t tag0 = (uint32_t)a.forced[0];
-    if (tid < D) s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
+    if (tid < D) {
+        s_ref[tid] = a.Xref[(uint64_t)tid * n + tag0];
+        if (blockIdx.x == 0 && a.out_pts && a.k > 0) a.out_pts[tid] = s_ref[tid];
+    }
     if (tid == 0) s_abort = 0;
     // outputs hold tags while sampling; kd-line tags are mapped afterwards
     if (blockIdx.x == 0 && tid == 0 && a.k > 0) {
@@ -1618,8 +1648,12 @@ __global__ void __launch_bounds__(kSmemThreads, 1) grid_sample_smem(GridSmemArgs
                 if (lane == 0) s_abort = 1;
             } else {
 #pragma unroll
-                for (int d = 0; d < D; ++d)
-                    if (lane == d) s_ref[d] = wc[d];  // static indices keep wc in registers
+                for (int d = 0; d < D; ++d) {
+                    if (lane == d) {  // static indices keep wc in registers
+                        s_ref[d] = wc[d];
+                        if (blockIdx.x == 0 && a.out_pts) a.out_pts[(t + 1) * D + d] = wc[d];
+                    }
+                }
                 if (blockIdx.x == 0 && lane == 0) {
                     a.out[t + 1] = KD ? tg : tg - a.id_offset;
                     if (a.trace) a.trace[t + 1] = forced ? INFINITY : key_dist(g);
@@ -1645,7 +1679,8 @@ constexpr int kNoFit = -1;
 template <int D, bool FMA>
 int sample_grid_smem(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint32_t np,
                      uint64_t k, const uint64_t* h_forced, uint32_t n_forced, uint64_t id_offset,
-                     uint64_t* d_out, float* d_trace, cudaStream_t stream, int sms, Scratch& sc) {
+                     uint64_t* d_out, float* d_trace, float* d_out_pts, cudaStream_t stream, int sms,
+                     Scratch& sc) {
     int rc;
     if (np == ~0u) {
         uint32_t h_np = 0;
@@ -1717,6 +1752,7 @@ int sample_grid_smem(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint
     a.id_offset = id_offset;
     a.out = d_out;
     a.trace = d_trace;
+    a.out_pts = d_out_pts;
     a.slots = slots;
     a.err = bt.err;
     a.counters = cnt;
@@ -1747,10 +1783,10 @@ int sample_grid_smem(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint
 template <int D, bool FMA>
 int sample_grid(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint32_t np,
                 uint64_t points_in_range, uint64_t k, const uint64_t* h_forced, uint32_t n_forced,
-                uint64_t id_offset, uint64_t* d_out, float* d_trace, cudaStream_t stream, int sms,
-                Scratch& sc) {
+                uint64_t id_offset, uint64_t* d_out, float* d_trace, float* d_out_pts,
+                cudaStream_t stream, int sms, Scratch& sc) {
     int rc = sample_grid_smem<D, FMA>(bt, n, kd, piece0, np, k, h_forced, n_forced, id_offset,
-                                      d_out, d_trace, stream, sms, sc);
+                                      d_out, d_trace, d_out_pts, stream, sms, sc);
     if (rc != kNoFit) return rc;
     uint32_t h_np = np;
     if (np == ~0u) {
@@ -1800,6 +1836,7 @@ int sample_grid(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint32_t 
     s.n_forced = n_forced;
     s.out = d_out;
     s.trace = d_trace;
+    s.out_pts = d_out_pts;
     s.slots = slots;
     s.err = bt.err;
     s.counters = cnt;
@@ -1844,6 +1881,7 @@ struct EngineCall {
     cudaStream_t stream;
     int sms;
     bool tie_last = false;  // bucket_fps_kdtree
+    float* d_out_pts = nullptr;  // null, or [k][D]: the sampled points (fused gather)
     // build-only mode (kd-line): host outputs
     uint64_t* h_perm;
     uint64_t* h_bucket_start;
@@ -1892,7 +1930,7 @@ int run_engine(const EngineCall& c) {
     // kd-tree: the start's tag is its reversed position
     const uint64_t f0 = c.tie_last ? n - 1 - c.h_forced[0] : c.h_forced[0];
     return sample_grid<D, FMA>(bt, n, c.kd, 0, ~0u, n, c.k, c.tie_last ? &f0 : c.h_forced,
-                               c.n_forced, 0, c.d_out, c.d_trace, c.stream, c.sms, sc);
+                               c.n_forced, 0, c.d_out, c.d_trace, c.d_out_pts, c.stream, c.sms, sc);
 }
 
 // Many clouds in one go: build all of them together, then one CTA per cloud
@@ -1908,6 +1946,7 @@ struct BatchCall {
     cudaStream_t stream;
     int sms;
     bool tie_last = false;            // bucket_fps_kdtree
+    float* d_out_pts = nullptr;       // null, or [sum k][D], cloud c at row out_off[c]
 };
 
 template <int D, bool FMA>
@@ -2048,6 +2087,7 @@ int run_batch(const BatchCall& bc) {
         a.out = bc.d_out;
         a.counters = cnt;
         a.err = bt.err;
+        a.out_pts = bc.d_out_pts;
         SamplerTimer timer;
         timer.begin(bc.stream);
         // both kinds at once: the clusters run on a side stream, concurrently
@@ -2109,6 +2149,7 @@ int run_batch(const BatchCall& bc) {
         const uint32_t np = h_cpiece[c + 1] - h_cpiece[c];
         if ((rc = sample_grid<D, FMA>(bt, n, bc.kd, h_cpiece[c], np, bc.off[c + 1] - bc.off[c],
                                       bc.k[c], &f, 1, bc.off[c], bc.d_out + out_off[c], nullptr,
+                                      bc.d_out_pts ? bc.d_out_pts + out_off[c] * D : nullptr,
                                       bc.stream, bc.sms, sc)))
             return rc;
     }

@@ -108,6 +108,7 @@ struct VanillaCall {
     float* d_trace;
     cudaStream_t stream;
     int sms;
+    float* d_out_pts = nullptr;  // null, or [k][dim]: the sampled points (fused gather)
 };
 int run_vanilla_nofma(const VanillaCall& c);
 int run_vanilla_fma(const VanillaCall& c);
@@ -126,7 +127,7 @@ int run_batch_fma(int dim, const BatchCall& c);
 int kdline_batch_device_capped(const float* d_points, const size_t* h_offsets, size_t n_clouds,
                                size_t dim, const size_t* h_n_samples, const size_t* h_start_idx,
                                const size_t* h_height, uint64_t* d_out, void* stream,
-                               int max_grid);
+                               int max_grid, float* d_out_pts = nullptr);
 
 // measurement counters (fpsgpu_stats_*)
 void stats_count_launch(uint64_t n = 1);

@@ -158,6 +158,41 @@ Indices bucket_fps_kdtree_sampling(FloatRows points, size_t n_samples, py::objec
     return out;
 }
 
+// Indices and the sampled points in one call (the gather fused into the
+// sampler): algo is FPSGPU_ALGO_FPS / _KDLINE / _KDTREE; starts holds one or
+// more start indices (one for the kd variants).  Returns (uint64 [K],
+// float32 [K, C]).  Argument checks are the ones of the matching function.
+py::tuple sample_points(int algo, FloatRows points, size_t n_samples, Indices starts,
+                        size_t height) {
+    if (points.ndim() != 2) throw py::value_error("points must be a 2D float32 array");
+    const ssize_t P = points.shape(0), C = points.shape(1);
+    const ssize_t m = starts.size();
+    if (m == 0) throw py::value_error("need at least one start index");
+    for (ssize_t i = 0; i < m; ++i)
+        if (starts.data()[i] >= static_cast<size_t>(P)) throw py::value_error("start_idx out of range");
+    if (n_samples == 0 || n_samples > static_cast<size_t>(P))
+        throw py::value_error("n_samples must be in [1, num_points]");
+    if (algo != FPSGPU_ALGO_FPS && m != 1) {
+        PyErr_SetString(PyExc_NotImplementedError, "Array of start indices not implemented yet");
+        throw py::error_already_set();
+    }
+    if (algo == FPSGPU_ALGO_KDLINE && height == 0) throw py::value_error("height must be >= 1");
+    Indices out(n_samples);
+    py::array_t<float> xyz({static_cast<ssize_t>(n_samples), C});
+    size_t* out_ptr = static_cast<size_t*>(out.mutable_data());
+    float* xyz_ptr = xyz.mutable_data();
+    const float* data = points.data();
+    const size_t* st = starts.data();
+    int rc;
+    {
+        py::gil_scoped_release nogil;
+        rc = fpsgpu_sample_points(algo, data, (size_t)P, (size_t)C, n_samples, st, (size_t)m, height,
+                                  out_ptr, xyz_ptr);
+    }
+    if (rc != 0) raise_gpu_failure("fpsgpu_sample_points", rc);
+    return py::make_tuple(out, xyz);
+}
+
 // Batched QuickFPS: clouds stored back to back in `points` (rows
 // [offsets[c], offsets[c+1]) form cloud c).  Returns one uint64 array with the
 // clouds' local indices back to back (cloud c at sum(n_samples[:c])).
@@ -288,6 +323,11 @@ PYBIND11_MODULE(_fpsample, m) {
                 np.ndarray[uint64]: sampled point indices.
     )pbdoc");
 
+    m.def("_sample_points", &sample_points,
+          "(algo, points, n_samples, starts uint64[], height) -> (indices, sampled points)");
+    m.attr("ALGO_FPS") = FPSGPU_ALGO_FPS;
+    m.attr("ALGO_KDLINE") = FPSGPU_ALGO_KDLINE;
+    m.attr("ALGO_KDTREE") = FPSGPU_ALGO_KDTREE;
     m.def("_bucket_fps_kdline_sampling_batch", &bucket_fps_kdline_sampling_batch,
           "many clouds in one GPU call: (points, offsets, n_samples, heights, starts) -> indices");
     m.def("_kdline_build", &kdline_build,

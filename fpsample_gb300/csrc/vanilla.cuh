@@ -36,6 +36,7 @@ struct VanillaArgs {
     uint32_t n_starts;
     uint64_t* out;
     float* trace;
+    float* out_pts;  // null, or [k][dim]: coordinates of every sample (fused gather)
     uint64_t* slots;
     int* err;
     int smem_cloud;  // resident kernel, G == 1: cloud copied to shared memory
@@ -81,7 +82,10 @@ __global__ void __launch_bounds__(kVanillaThreads, 1) vanilla_resident(VanillaAr
         a.out[0] = pos;
         if (a.trace) a.trace[0] = INFINITY;
     }
-    if (tid < D) s_ref[tid] = a.pts[pos * D + tid];
+    if (tid < D) {
+        s_ref[tid] = a.pts[pos * D + tid];
+        if (blockIdx.x == 0 && a.out_pts) a.out_pts[tid] = s_ref[tid];
+    }
     __syncthreads();
 
     uint32_t xround = 0;
@@ -120,7 +124,11 @@ __global__ void __launch_bounds__(kVanillaThreads, 1) vanilla_resident(VanillaAr
             if (!ok) {
                 if (lane == 0) s_abort = 1;
             } else {
-                if (lane < D) s_ref[lane] = src[pos * D + lane];
+                if (lane < D) {
+                    const float v = src[pos * D + lane];
+                    s_ref[lane] = v;
+                    if (blockIdx.x == 0 && a.out_pts) a.out_pts[t * D + lane] = v;
+                }
                 if (blockIdx.x == 0 && lane == 0) {
                     a.out[t] = pos;
                     if (a.trace) a.trace[t] = forced ? INFINITY : key_dist(g);
@@ -160,7 +168,10 @@ __global__ void __launch_bounds__(kVanillaThreads, 1) vanilla_stream(VanillaArgs
         a.out[0] = pos;
         if (a.trace) a.trace[0] = INFINITY;
     }
-    for (int d = tid; d < dim; d += T) s_ref[d] = X[(uint64_t)d * n + pos];
+    for (int d = tid; d < dim; d += T) {
+        s_ref[d] = X[(uint64_t)d * n + pos];
+        if (blockIdx.x == 0 && a.out_pts) a.out_pts[d] = s_ref[d];
+    }
     __syncthreads();
 
     uint32_t xround = 0;
@@ -216,7 +227,11 @@ __global__ void __launch_bounds__(kVanillaThreads, 1) vanilla_stream(VanillaArgs
             if (!ok) {
                 if (lane == 0) s_abort = 1;
             } else {
-                for (int d = lane; d < dim; d += 32) s_ref[d] = X[(uint64_t)d * n + pos];
+                for (int d = lane; d < dim; d += 32) {
+                    const float v = X[(uint64_t)d * n + pos];
+                    s_ref[d] = v;
+                    if (blockIdx.x == 0 && a.out_pts) a.out_pts[t * (uint64_t)dim + d] = v;
+                }
                 if (blockIdx.x == 0 && lane == 0) {
                     a.out[t] = pos;
                     if (a.trace) a.trace[t] = forced ? INFINITY : key_dist(g);
@@ -259,6 +274,7 @@ int run_vanilla_d(const VanillaCall& c) {
     a.n_starts = c.n_starts;
     a.out = c.d_out;
     a.trace = c.d_trace;
+    a.out_pts = c.d_out_pts;
     int rc;
     uint64_t* d_starts;
     if ((rc = sc.alloc(&d_starts, c.n_starts))) return rc;

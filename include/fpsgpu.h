@@ -41,6 +41,11 @@ extern "C" {
 #define FPSGPU_FP_NOFMA 0
 #define FPSGPU_FP_FMA 1
 
+/* algorithm selector of fpsgpu_sample_points* */
+#define FPSGPU_ALGO_FPS 0      /* vanilla FPS (fpsgpu_fps), any number of starts */
+#define FPSGPU_ALGO_KDLINE 1   /* bucket_fps_kdline, one start, `height`         */
+#define FPSGPU_ALGO_KDTREE 2   /* bucket_fps_kdtree, one start                    */
+
 /*
  * Replaces the reference's C ABI of the same name and signature
  * (src/wrapper.hpp:118-132): QuickFPS with a kd-line bucket tree of `height`.
@@ -206,6 +211,28 @@ const char *fpsgpu_last_error(void);
 
 /* library version string */
 const char *fpsgpu_version(void);
+
+/* ---- sampled points: the gather that callers do next, fused -------------
+ * What callers of FPS do next is the gather pc[idx]: the sampled coordinates
+ * are what the next stage consumes.  These calls return, beside
+ * the indices, the sampled points themselves as n_samples x dim floats,
+ * row-major like the input, written by the sampler at the moment each point
+ * is chosen (it holds the winner's coordinates anyway): no second pass over
+ * the cloud, no extra launch.  sampled_points / d_out_points may be NULL.
+ * Indices are the same as from the calls above for the same algorithm. */
+int fpsgpu_sample_points(int algo, const float *raw_data, size_t n_points, size_t dim,
+                         size_t n_samples, const size_t *start_idx, size_t n_start,
+                         size_t height, size_t *sampled_point_indices, float *sampled_points);
+int fpsgpu_sample_points_device(int algo, const float *d_points, size_t n_points, size_t dim,
+                                size_t n_samples, const size_t *h_start, size_t n_start,
+                                size_t height, uint64_t *d_out, float *d_out_points,
+                                void *stream);
+/* fpsgpu_kdline_batch_device plus the sampled points ([sum n_samples][dim],
+ * cloud c's rows after the rows of clouds 0..c-1). */
+int fpsgpu_kdline_batch_points_device(const float *d_points, const size_t *h_offsets,
+                                      size_t n_clouds, size_t dim, const size_t *h_n_samples,
+                                      const size_t *h_start_idx, const size_t *h_height,
+                                      uint64_t *d_out, float *d_out_points, void *stream);
 
 /* ---- diagnostics (no reference counterpart) -------------------------------
  * Read bandwidth of an on-chip level of the current GPU, in GB/s, measured by a

@@ -245,8 +245,58 @@ def test_beyond_register_capacity_uses_streaming_sampler():
     v = fps.fps_sampling(pts, 64, 7)
     np.testing.assert_array_equal(v[:8], ORACLE.fps(pts, 8, 7))
     assert len(np.unique(v)) == 64
+    idx, xyz = fps.fps_sampling_points(pts, 64, 7)
+    np.testing.assert_array_equal(idx, v)
+    np.testing.assert_array_equal(xyz, pts[v.astype(np.int64)])
     kd = fps.bucket_fps_kdline_sampling(pts, 64, 1, 7)
     np.testing.assert_array_equal(kd[:24], ORACLE.kdline(pts, 24, 1, 7))
+
+
+@pytest.mark.parametrize("n,d", [(3000, 3), (20000, 3), (300_000, 3), (5000, 12),
+                                 (2_500_000, 2)])
+def test_sampled_points_are_the_gather(n, d, mode):
+    """The *_points calls return the same indices as the plain calls and
+    pc[indices] bit for bit, on every sampler: resident and streaming vanilla,
+    one CTA, a cluster, forced starts on the grid, the register grid."""
+    rng = np.random.default_rng(n + d)
+    pts = (rng.standard_normal((n, d)) * 7).astype(np.float32)
+    k = 700
+    idx, xyz = fps.fps_sampling_points(pts, k, 11)
+    np.testing.assert_array_equal(idx, fps.fps_sampling(pts, k, 11))
+    np.testing.assert_array_equal(xyz, pts[idx.astype(np.int64)])
+    idx, xyz = fps.fps_sampling_points(pts, k, [11, 5, 999])
+    np.testing.assert_array_equal(idx, fps.fps_sampling(pts, k, [11, 5, 999]))
+    np.testing.assert_array_equal(xyz, pts[idx.astype(np.int64)])
+    if d <= 8:
+        idx, xyz = fps.bucket_fps_kdline_sampling_points(pts, k, 7, 3)
+        np.testing.assert_array_equal(idx, fps.bucket_fps_kdline_sampling(pts, k, 7, 3))
+        np.testing.assert_array_equal(xyz, pts[idx.astype(np.int64)])
+        idx, xyz = fps.bucket_fps_kdtree_sampling_points(pts, k, 3)
+        np.testing.assert_array_equal(idx, fps.bucket_fps_kdtree_sampling(pts, k, 3))
+        np.testing.assert_array_equal(xyz, pts[idx.astype(np.int64)])
+
+
+def test_batch_points_are_the_gather():
+    torch = pytest.importorskip("torch")
+    clouds, ks, hs, ss = _batch_clouds(77, 12, 300, 30000)
+    clouds.append(W.gmm_cloud(400_000, seed=9))  # more pieces than one CTA: a cluster
+    ks.append(1500)
+    hs.append(7)
+    ss.append(5)
+    sizes = [p.shape[0] for p in clouds]
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    t = torch.from_numpy(np.concatenate(clouds)).cuda()
+    out = torch.empty(sum(ks), dtype=torch.int64, device="cuda")
+    xyz = torch.empty((sum(ks), 3), dtype=torch.float32, device="cuda")
+    capi.kdline_batch_points_device(t.data_ptr(), off, 3, ks, hs, ss, out.data_ptr(),
+                                    xyz.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    got, pts_got = out.cpu().numpy(), xyz.cpu().numpy()
+    want = capi.kdline_batch(clouds, ks, hs, ss)
+    kb = np.concatenate([[0], np.cumsum(ks)])
+    for c, p in enumerate(clouds):
+        np.testing.assert_array_equal(got[kb[c]:kb[c + 1]].astype(np.uint64), want[c])
+        np.testing.assert_array_equal(pts_got[kb[c]:kb[c + 1]], p[want[c].astype(np.int64)])
 
 
 def _batch_clouds(seed, count, lo, hi, d=3):
