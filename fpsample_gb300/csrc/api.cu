@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <atomic>
 #include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -91,6 +92,43 @@ int launch_persistent(const void* func, int grid, int block, void** args, size_t
     return FPSGPU_OK;
 }
 
+namespace {
+thread_local cudaMemPool_t t_pool = nullptr;
+std::mutex g_attr_mu;
+std::set<std::pair<int, const void*>> g_smem_raised, g_cluster16;
+}
+
+// Kernel attributes are set once per (device, kernel) and never changed again:
+// the dynamic shared-memory limit goes straight to the device's opt-in maximum,
+// so concurrent calls (server workers) never change an attribute of a kernel
+// that another stream is running.
+int allow_max_smem(const void* func) {
+    int dev = 0;
+    FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    if (g_smem_raised.count({dev, func})) return FPSGPU_OK;
+    int optin = 0;
+    FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa{};
+    FPSGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, func));
+    FPSGPU_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         optin - (int)fa.sharedSizeBytes));
+    g_smem_raised.insert({dev, func});
+    return FPSGPU_OK;
+}
+
+int allow_cluster16(const void* func) {
+    int dev = 0;
+    FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_attr_mu);
+    if (g_cluster16.count({dev, func})) return FPSGPU_OK;
+    FPSGPU_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    g_cluster16.insert({dev, func});
+    return FPSGPU_OK;
+}
+void set_thread_pool(cudaMemPool_t pool) { t_pool = pool; }
+cudaMemPool_t thread_pool() { return t_pool; }
+
 // Cluster size of the batched engine's cluster sampler: FPSGPU_CLUSTER_SIZE
 // (1 turns clusters off; 2, 4, 8 or 16), default 8; clouds that need more CTAs
 // get the next power of two up to 16.
@@ -120,9 +158,9 @@ uint32_t cluster_min_pieces() {
 // How many clusters of `cl` CTAs of `func` can be resident at once (0: none).
 int cluster_capacity(const void* func, int cl, int block, size_t smem, int* out) {
     *out = 0;
-    if (cl > 8)
-        FPSGPU_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    FPSGPU_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int rc;
+    if (cl > 8 && (rc = allow_cluster16(func))) return rc;
+    if ((rc = allow_max_smem(func))) return rc;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -144,10 +182,10 @@ int cluster_capacity(const void* func, int cl, int block, size_t smem, int* out)
     return FPSGPU_OK;
 }
 
-// Persistent cluster launch: min(items, resident clusters) clusters of `cl`
-// CTAs; the kernel's clusters take items from a queue.
+// Persistent cluster launch: min(items, resident clusters, max_ctas / cl)
+// clusters of `cl` CTAs; the kernel's clusters take items from a queue.
 int launch_clustered(const void* func, int items, int cl, int block, void** args, size_t smem,
-                     cudaStream_t stream) {
+                     cudaStream_t stream, int max_ctas) {
     int maxc = 0;
     int rc = cluster_capacity(func, cl, block, smem, &maxc);
     if (rc) return rc;
@@ -159,7 +197,8 @@ int launch_clustered(const void* func, int items, int cl, int block, void** args
     at[0].val.clusterDim.x = (unsigned)cl;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3((unsigned)(std::min(items, maxc) * cl));
+    const int ncl = std::max(1, std::min({items, maxc, max_ctas > 0 ? max_ctas / cl : maxc}));
+    cfg.gridDim = dim3((unsigned)(ncl * cl));
     cfg.blockDim = dim3((unsigned)block);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
@@ -707,7 +746,7 @@ namespace fpsgpu {
 int kdline_batch_device_capped(const float* d_points, const size_t* h_offsets, size_t n_clouds,
                                size_t dim, const size_t* h_n_samples, const size_t* h_start_idx,
                                const size_t* h_height, uint64_t* d_out, void* stream,
-                               int max_grid, float* d_out_pts) {
+                               int max_grid, float* d_out_pts, int min_cluster) {
     clear_error();
     if (n_clouds == 0) return FPSGPU_OK;
     if (!h_offsets || !h_n_samples || !h_start_idx || !h_height)
@@ -737,6 +776,7 @@ int kdline_batch_device_capped(const float* d_points, const size_t* h_offsets, s
     b.kd = true;
     b.d_out = d_out;
     b.d_out_pts = d_out_pts;
+    b.min_cluster = min_cluster;
     b.stream = s;
     b.sms = max_grid > 0 && max_grid < ctx.sms ? max_grid : ctx.sms;
     return fp_mode() == FPSGPU_FP_FMA ? run_batch_fma((int)dim, b) : run_batch_nofma((int)dim, b);

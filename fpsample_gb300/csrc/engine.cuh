@@ -1758,7 +1758,7 @@ int sample_grid_smem(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint
     a.counters = cnt;
     const void* kern = kd ? (const void*)grid_sample_smem<D, FMA, true>
                           : (const void*)grid_sample_smem<D, FMA, false>;
-    FPSGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (int arc = allow_max_smem((const void*)kern)) return arc;
     void* args[] = {&a};
     SamplerTimer timer;
     timer.begin(stream);
@@ -1847,7 +1847,7 @@ int sample_grid(const Built& bt, uint64_t n, bool kd, uint32_t piece0, uint32_t 
         const void* kern = kd ? (const void*)grid_sample_reg<D, FMA, true>
                               : (const void*)grid_sample_reg<D, FMA, false>;
         const size_t smem = grid_reg_smem_bytes(D);
-        FPSGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (int arc = allow_max_smem((const void*)kern)) return arc;
         if ((rc = launch_persistent(kern, (int)G, kRegThreads, args, smem, stream, G > 1))) return rc;
     } else {
         const void* kern = kd ? (const void*)fps_sample<D, FMA, true> : (const void*)fps_sample<D, FMA, false>;
@@ -1947,6 +1947,10 @@ struct BatchCall {
     int sms;
     bool tie_last = false;            // bucket_fps_kdtree
     float* d_out_pts = nullptr;       // null, or [sum k][D], cloud c at row out_off[c]
+    // smallest cluster for clouds that need one (0: the latency default,
+    // cluster_size_for_batch(); 1: just as many CTAs as the pieces need, which
+    // leaves more SMs to other work, e.g. in the server)
+    int min_cluster = 0;
 };
 
 template <int D, bool FMA>
@@ -1990,7 +1994,7 @@ int run_batch(const BatchCall& bc) {
     }
     const size_t avail = (size_t)smem_optin - static_smem - 256;
     const uint32_t cap_max = (uint32_t)batch_slots(D) * batch_threads(D);
-    const int want_cluster = cluster_size_for_batch();
+    const int want_cluster = bc.min_cluster > 0 ? bc.min_cluster : cluster_size_for_batch();
     const uint32_t promote = cluster_min_pieces();
     std::vector<uint64_t> out_off(C), tag0(C);
     std::vector<uint32_t> small, clustered, big;
@@ -2006,7 +2010,7 @@ int run_batch(const BatchCall& bc) {
         const uint32_t np = h_cpiece[c + 1] - h_cpiece[c];
         const uint64_t nc = bc.off[c + 1] - bc.off[c];
         if (bc.k[c] == 0) continue;
-        const bool to_cluster = want_cluster > 1 && np <= (uint64_t)kMaxCluster * cap_max &&
+        const bool to_cluster = cluster_size_for_batch() > 1 && np <= (uint64_t)kMaxCluster * cap_max &&
                                 nc <= kBatchMaxCloudPoints;
         if (np <= cap_max && !(to_cluster && promote > 0 && np >= promote)) {
             small.push_back((uint32_t)c);
@@ -2105,7 +2109,7 @@ int run_batch(const BatchCall& bc) {
             b.mcap = 0;
             void* args[] = {&b};
             if ((rc = launch_clustered(cl_kern, (int)clustered.size(), cl, batch_threads(D), args,
-                                       cl_smem, both ? side.s : bc.stream)))
+                                       cl_smem, both ? side.s : bc.stream, bc.sms)))
                 return rc;
         }
         if (!small.empty()) {
@@ -2122,8 +2126,7 @@ int run_batch(const BatchCall& bc) {
             const size_t smem = batch_smem_bytes(D, cap, a.mcap);
             const void* kern = bc.kd ? (const void*)batch_sample<D, FMA, true, false>
                                      : (const void*)batch_sample<D, FMA, false, false>;
-            FPSGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem));
+            if (int arc = allow_max_smem((const void*)kern)) return arc;
             int per_sm = 0;
             FPSGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, batch_threads(D), smem));
             int slots = std::max(1, per_sm) * bc.sms;

@@ -37,6 +37,13 @@ int current_ctx(DevCtx* ctx);
 
 // Stream-ordered scratch: every allocation is released with cudaFreeAsync on
 // the same stream when the object goes out of scope.
+// The memory pool that stream-ordered scratch of the calling thread comes from
+// (null: the device's default pool).  Server workers each use their own pool:
+// the default pool may make one stream wait for another stream's work in order
+// to reuse memory freed there, which would chain independent batches together.
+void set_thread_pool(cudaMemPool_t pool);
+cudaMemPool_t thread_pool();
+
 class Scratch {
    public:
     explicit Scratch(cudaStream_t s) : s_(s) {}
@@ -49,7 +56,9 @@ class Scratch {
     int alloc(T** out, size_t count) {
         void* p = nullptr;
         size_t bytes = count ? count * sizeof(T) : sizeof(T);
-        cudaError_t e = cudaMallocAsync(&p, bytes, s_);
+        cudaMemPool_t pool = thread_pool();
+        cudaError_t e = pool ? cudaMallocFromPoolAsync(&p, bytes, pool, s_)
+                             : cudaMallocAsync(&p, bytes, s_);
         if (e != cudaSuccess)
             return set_error(FPSGPU_ERR_CUDA, "cudaMallocAsync(%zu bytes) failed: %s", bytes,
                              cudaGetErrorString(e));
@@ -127,7 +136,7 @@ int run_batch_fma(int dim, const BatchCall& c);
 int kdline_batch_device_capped(const float* d_points, const size_t* h_offsets, size_t n_clouds,
                                size_t dim, const size_t* h_n_samples, const size_t* h_start_idx,
                                const size_t* h_height, uint64_t* d_out, void* stream,
-                               int max_grid, float* d_out_pts = nullptr);
+                               int max_grid, float* d_out_pts = nullptr, int min_cluster = 0);
 
 // measurement counters (fpsgpu_stats_*)
 void stats_count_launch(uint64_t n = 1);
@@ -147,11 +156,15 @@ struct SamplerTimer {
 // cooperative launch helper: refuses grids that cannot be co-resident
 int launch_persistent(const void* func, int grid, int block, void** args, size_t smem,
                       cudaStream_t stream, bool cooperative);
+// one-time kernel attributes (see api.cu)
+int allow_max_smem(const void* func);
+int allow_cluster16(const void* func);
+
 // thread-block cluster launches (batched engine's cluster sampler)
 int cluster_size_for_batch();
 uint32_t cluster_min_pieces();
 int cluster_capacity(const void* func, int cl, int block, size_t smem, int* out);
 int launch_clustered(const void* func, int items, int cl, int block, void** args, size_t smem,
-                     cudaStream_t stream);
+                     cudaStream_t stream, int max_ctas = 0);
 
 }  // namespace fpsgpu

@@ -31,7 +31,9 @@
 namespace fpsgpu {
 namespace {
 
-constexpr size_t kSmallPoints = 262144;
+// at most 131072 points: every small request fits one CTA of the batched
+// sampler (2048 pieces), so no small batch ever waits for a cluster
+constexpr size_t kSmallPoints = 131072;
 constexpr size_t kMaxBatch = 64;
 
 double now_ms() {
@@ -74,10 +76,29 @@ struct Server {
     void worker(int cls) {
         cudaSetDevice(device);
         cudaStream_t stream;
-        if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return;
-        float* h_pts = nullptr;
-        uint64_t* h_out = nullptr;
-        size_t cap_pts = 0, cap_out = 0;
+        // small requests first: their streams get the device's highest priority,
+        // so their CTAs are scheduled ahead of the large class's as SMs free up
+        int lo_prio = 0, hi_prio = 0;
+        cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+        if (cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking,
+                                         cls == 0 ? hi_prio : lo_prio) != cudaSuccess)
+            return;
+        // a memory pool of this worker's own: no allocation of this worker can
+        // be made to wait for another worker's batch
+        cudaMemPool_t pool = nullptr;
+        {
+            cudaMemPoolProps props = {};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = device;
+            if (cudaMemPoolCreate(&pool, &props) == cudaSuccess) {
+                uint64_t keep = budget;  // keep freed memory for the next batch
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            } else {
+                pool = nullptr;
+            }
+        }
+        set_thread_pool(pool);
         for (;;) {
             std::vector<Request*> batch;
             size_t bytes = 0;
@@ -103,67 +124,49 @@ struct Server {
                 const double t = now_ms();
                 for (Request* r : batch) r->t_admit = t;
             }
-            // pack the batch into pinned staging, one upload, one batched call
+            // upload every request straight from its caller's buffer into the
+            // batch's device buffer: no pinned staging, whose cudaFreeHost on
+            // growth would wait for every other worker's kernels
             const size_t dim = batch[0]->dim;
-            std::vector<size_t> off(batch.size() + 1, 0), ks, starts, heights;
-            size_t ktot = 0;
+            std::vector<size_t> off(batch.size() + 1, 0), koff(batch.size() + 1, 0), ks, starts,
+                heights;
             for (size_t i = 0; i < batch.size(); ++i) {
                 off[i + 1] = off[i] + batch[i]->n;
+                koff[i + 1] = koff[i] + batch[i]->k;
                 ks.push_back(batch[i]->k);
                 starts.push_back(batch[i]->start);
                 heights.push_back(batch[i]->height);
-                ktot += batch[i]->k;
             }
             int rc = FPSGPU_OK;
-            const size_t npts = off.back();
-            if (npts * dim > cap_pts) {
-                if (h_pts) cudaFreeHost(h_pts);
-                cap_pts = npts * dim * 2;
-                if (cudaHostAlloc((void**)&h_pts, cap_pts * sizeof(float), cudaHostAllocDefault) != cudaSuccess) {
-                    h_pts = nullptr;
-                    cap_pts = 0;
-                    rc = set_error(FPSGPU_ERR_CUDA, "pinned staging allocation failed");
-                }
-            }
-            if (!rc && ktot > cap_out) {
-                if (h_out) cudaFreeHost(h_out);
-                cap_out = ktot * 2;
-                if (cudaHostAlloc((void**)&h_out, cap_out * sizeof(uint64_t), cudaHostAllocDefault) != cudaSuccess) {
-                    h_out = nullptr;
-                    cap_out = 0;
-                    rc = set_error(FPSGPU_ERR_CUDA, "pinned staging allocation failed");
-                }
-            }
+            const size_t npts = off.back(), ktot = koff.back();
             float* d_pts = nullptr;
             uint64_t* d_out = nullptr;
-            if (!rc) {
-                for (size_t i = 0; i < batch.size(); ++i)
-                    std::memcpy(h_pts + off[i] * dim, batch[i]->pts, batch[i]->n * dim * sizeof(float));
-                if (cudaMallocAsync((void**)&d_pts, npts * dim * sizeof(float), stream) != cudaSuccess ||
-                    cudaMallocAsync((void**)&d_out, ktot * sizeof(uint64_t), stream) != cudaSuccess)
-                    rc = set_error(FPSGPU_ERR_CUDA, "device allocation for a batch failed");
-            }
-            if (!rc && cudaMemcpyAsync(d_pts, h_pts, npts * dim * sizeof(float), cudaMemcpyHostToDevice,
-                                       stream) != cudaSuccess)
-                rc = set_error(FPSGPU_ERR_CUDA, "upload failed");
+            auto dev_alloc = [&](void** p, size_t bytes) {
+                return pool ? cudaMallocFromPoolAsync(p, bytes, pool, stream)
+                            : cudaMallocAsync(p, bytes, stream);
+            };
+            if (dev_alloc((void**)&d_pts, npts * dim * sizeof(float)) != cudaSuccess ||
+                dev_alloc((void**)&d_out, ktot * sizeof(uint64_t)) != cudaSuccess)
+                rc = set_error(FPSGPU_ERR_CUDA, "device allocation for a batch failed");
+            for (size_t i = 0; i < batch.size() && !rc; ++i)
+                if (cudaMemcpyAsync(d_pts + off[i] * dim, batch[i]->pts,
+                                    batch[i]->n * dim * sizeof(float), cudaMemcpyHostToDevice,
+                                    stream) != cudaSuccess)
+                    rc = set_error(FPSGPU_ERR_CUDA, "upload failed");
             if (!rc)
                 rc = kdline_batch_device_capped(d_pts, off.data(), batch.size(), dim, ks.data(),
                                                 starts.data(), heights.data(), d_out, stream,
-                                                grid_cap);
-            if (!rc && cudaMemcpyAsync(h_out, d_out, ktot * sizeof(uint64_t), cudaMemcpyDeviceToHost,
-                                       stream) != cudaSuccess)
-                rc = set_error(FPSGPU_ERR_CUDA, "download failed");
+                                                grid_cap, nullptr, /*min_cluster=*/1);
+            for (size_t i = 0; i < batch.size() && !rc; ++i)
+                if (cudaMemcpyAsync(batch[i]->out, d_out + koff[i], batch[i]->k * sizeof(uint64_t),
+                                    cudaMemcpyDeviceToHost, stream) != cudaSuccess)
+                    rc = set_error(FPSGPU_ERR_CUDA, "download failed");
             if (d_pts) cudaFreeAsync(d_pts, stream);
             if (d_out) cudaFreeAsync(d_out, stream);
             if (cudaStreamSynchronize(stream) != cudaSuccess && !rc)
                 rc = set_error(FPSGPU_ERR_CUDA, "batch failed on the device");
             batches.fetch_add(1);
             {
-                size_t o = 0;
-                for (Request* r : batch) {
-                    if (!rc) std::memcpy(r->out, h_out + o, r->k * sizeof(uint64_t));
-                    o += r->k;
-                }
                 std::lock_guard<std::mutex> lk(mu);
                 const double t = now_ms();
                 for (Request* r : batch) {
@@ -176,8 +179,9 @@ struct Server {
             cv_done.notify_all();
             cv_work.notify_all();
         }
-        if (h_pts) cudaFreeHost(h_pts);
-        if (h_out) cudaFreeHost(h_out);
+        cudaStreamSynchronize(stream);
+        set_thread_pool(nullptr);
+        if (pool) cudaMemPoolDestroy(pool);
         cudaStreamDestroy(stream);
     }
 };
@@ -202,6 +206,7 @@ int fpsgpu_server_create(size_t max_device_bytes, int small_workers, int large_w
     int sms = 0;
     FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     s->grid_cap = std::max(1, sms / (large_workers + 1));
+
     for (int i = 0; i < small_workers; ++i) s->workers.emplace_back(&Server::worker, s, 0);
     for (int i = 0; i < large_workers; ++i) s->workers.emplace_back(&Server::worker, s, 1);
     *out = s;

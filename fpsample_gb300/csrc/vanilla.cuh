@@ -257,8 +257,7 @@ int launch_resident(const VanillaCall& c, VanillaArgs a, int G) {
     size_t smem = a.smem_cloud ? (size_t)c.n * D * sizeof(float) : 0;
     // static + dynamic shared memory above 48 KB needs the opt-in attribute
     if (smem > 0)
-        FPSGPU_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem));
+        if (int arc = allow_max_smem((const void*)kern)) return arc;
     void* args[] = {&a};
     return launch_persistent((const void*)kern, G, kVanillaThreads, args, smem, c.stream, G > 1);
 }
@@ -341,8 +340,7 @@ int run_vanilla_d(const VanillaCall& c) {
         auto kern = vanilla_stream<D, FMA>;
         size_t smem = D > 0 ? 0 : (size_t)c.dim * sizeof(float);
         if (smem > 0)
-            FPSGPU_CUDA_TRY(cudaFuncSetAttribute(
-                kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            if (int arc = allow_max_smem((const void*)kern)) return arc;
         void* args[] = {&a};
         timer.begin(c.stream);
         if ((rc = launch_persistent((const void*)kern, G, kVanillaThreads, args, smem, c.stream,
