@@ -109,6 +109,23 @@ def truncated_k(algo: str, n: int, k: int):
     return None
 
 
+def max_over_ranks(x: float, world: int, device) -> float:
+    """The largest x over all ranks (the step time of the slowest replica)."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank: int, world: int, seconds: float) -> float:
+    """Whole-job throughput of N replicas: every rank processes its own copy of
+    the workload, the job lasts as long as the slowest rank."""
+    return units_per_rank * world / seconds
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -427,12 +444,8 @@ def run_gpu_arm(args):
     capi.stats_timing(False)
     st = capi.stats()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    my_ms = statistics.mean(step_ms)
-    t = torch.tensor([my_ms], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms = float(t.item())
-    value = len(clouds) * world / (ms / 1e3)
+    ms = max_over_ranks(statistics.mean(step_ms), world, dev)
+    value = job_value(len(clouds), world, ms / 1e3)
 
     # e2e through the public API (host arrays, copies inside the timed region)
     e2e_steps = max(1, min(args.steps, 3))
@@ -442,11 +455,8 @@ def run_gpu_arm(args):
     for _ in range(e2e_steps):
         step_e2e()
     barrier()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    te = torch.tensor([e2e_s], device=dev)
-    if world > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_v = len(clouds) * world / float(te.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world, dev)
+    e2e_v = job_value(len(clouds), world, e2e_s)
 
     # the plain one-call-per-cloud GPU form on the same data, for comparison
     barrier()
