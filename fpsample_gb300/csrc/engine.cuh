@@ -27,7 +27,7 @@
 //        - the two-pointer partition (KDTreeBase.h:123-149) in parallel: with
 //          L = #(x < split), the k-th element >= split in [s, s+L) trades
 //          places with the k-th element < split counted from the right end of
-//          [s+L, e); ranks from block-wide ballot scans; split point L clamped
+//          [s+L, e); ranks from warp-segment ballot scans; split point L clamped
 //          to [1, count-1]; leaf at depth == height or one point
 //          (KDLineTree.h:37-39).
 //      Then a snapshot: Xref = coordinates by permuted position, idsnap =
@@ -159,16 +159,57 @@ __global__ void build_prepare(const float* __restrict__ pts, BuildArgs a, const 
     }
 }
 
-// Splits the nodes of one level, one CTA per node.
+// Exclusive offsets of this warp's two counts among the block's warps (warp
+// order) and the block totals; one __syncthreads.  s_w holds 2 x 32 words and
+// must not be reused before the next __syncthreads.
+__device__ __forceinline__ void warp_offsets2(uint32_t c0, uint32_t c1, uint32_t* s_w, uint32_t& o0,
+                                              uint32_t& o1, uint32_t& t0, uint32_t& t1) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    if (lane == 0) {
+        s_w[warp] = c0;
+        s_w[32 + warp] = c1;
+    }
+    __syncthreads();
+    uint32_t a = lane < nwarps ? s_w[lane] : 0u, b = lane < nwarps ? s_w[32 + lane] : 0u;
+    uint32_t va = a, vb = b;  // inclusive scans over the warp counts
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t ua = __shfl_up_sync(kFull, va, o), ub = __shfl_up_sync(kFull, vb, o);
+        if (lane >= o) {
+            va += ua;
+            vb += ub;
+        }
+    }
+    t0 = __shfl_sync(kFull, va, 31);
+    t1 = __shfl_sync(kFull, vb, 31);
+    o0 = __shfl_sync(kFull, va - a, warp);
+    o1 = __shfl_sync(kFull, vb - b, warp);
+}
+
+// Warp w's share [lo, hi) of an index range [0, len) cut into nwarps
+// contiguous, 32-aligned segments (coalesced within the warp).
+__device__ __forceinline__ void warp_segment(uint32_t len, uint32_t& lo, uint32_t& hi) {
+    const uint32_t nwarps = blockDim.x >> 5, warp = threadIdx.x >> 5;
+    const uint32_t seg = ((len + nwarps - 1) / nwarps + 31u) & ~31u;
+    lo = min(len, warp * seg);
+    hi = min(len, lo + seg);
+}
+
+// Splits the nodes of one level, one CTA of T threads per node.
 // EXACT: the reference's kd-line rule (bit-exact permutation).
 // !EXACT: refinement (any rule; mean of the widest dimension, or halving).
-template <int D, bool EXACT>
-__global__ void __launch_bounds__(EXACT ? kBuildThreads : kRefineThreads)
-    split_kernel(BuildArgs a, int force_leaf) {
+// Every pass over the node streams it with U independent loads per thread in
+// flight; the partition ranks come from warp-contiguous segments (two passes:
+// counts, one block-wide scan of the warp counts, then ranks by ballot), so a
+// node costs a handful of __syncthreads whatever its size.
+template <int D, bool EXACT, int T>
+__global__ void __launch_bounds__(T) split_kernel(BuildArgs a, int force_leaf) {
     constexpr int RING = EXACT ? kSumChunk : 4;
+    constexpr int U = D <= 4 ? 4 : 2;  // loads in flight per thread and pass
     __shared__ __align__(16) float s_ring[2][RING];
     __shared__ float s_lo[32][D], s_hi[32][D];
     __shared__ uint32_t s_w[2 * 32];
+    __shared__ uint32_t s_w2[2 * 32];
     __shared__ float s_fw[32];
     __shared__ float s_split;
     __shared__ int s_dim;
@@ -179,15 +220,14 @@ __global__ void __launch_bounds__(EXACT ? kBuildThreads : kRefineThreads)
     const uint4 nd = a.cur[blockIdx.x];
     const uint32_t s = nd.x, e = nd.y, cntn = e - s;
     const uint64_t n = a.n;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-    const uint32_t T = blockDim.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = T / 32;
 
     if (!EXACT && force_leaf) {  // last refinement level: everything left is a piece
         if (tid == 0) a.flag[s] = 1;
         return;
     }
 
-    // 1. bounding box and split dimension
+    // 1. bounding box and split dimension (min/max: order-free, NaN ignored)
     {
         float lo[D], hi[D];
 #pragma unroll
@@ -195,12 +235,21 @@ __global__ void __launch_bounds__(EXACT ? kBuildThreads : kRefineThreads)
             lo[d] = FLT_MAX;
             hi[d] = -FLT_MAX;
         }
-        for (uint32_t p = s + tid; p < e; p += T) {
+        for (uint32_t b = s + tid; b < e; b += T * U) {
+            float v[U][D];
 #pragma unroll
-            for (int d = 0; d < D; ++d) {
-                float v = a.X[(uint64_t)d * n + p];
-                lo[d] = fminf(lo[d], v);
-                hi[d] = fmaxf(hi[d], v);
+            for (int u = 0; u < U; ++u) {
+                const uint32_t p = b + u * T;
+#pragma unroll
+                for (int d = 0; d < D; ++d) v[u][d] = p < e ? a.X[(uint64_t)d * n + p] : NAN;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    lo[d] = fminf(lo[d], v[u][d]);
+                    hi[d] = fmaxf(hi[d], v[u][d]);
+                }
             }
         }
 #pragma unroll
@@ -268,11 +317,22 @@ __global__ void __launch_bounds__(EXACT ? kBuildThreads : kRefineThreads)
         if (tid == 0) s_split = __fdiv_rn(acc, __uint2float_rn(cntn));
         __syncthreads();
     } else {
-        float part = 0.0f;
-        for (uint32_t p = s + tid; p < e; p += T) part += col[p];
+        float part[U];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(kFull, part, o);
-        if (lane == 0) s_fw[warp] = part;
+        for (int u = 0; u < U; ++u) part[u] = 0.0f;
+        for (uint32_t b = s + tid; b < e; b += T * U) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t p = b + u * T;
+                part[u] += p < e ? col[p] : 0.0f;
+            }
+        }
+        float tot_t = 0.0f;
+#pragma unroll
+        for (int u = 0; u < U; ++u) tot_t += part[u];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) tot_t += __shfl_xor_sync(kFull, tot_t, o);
+        if (lane == 0) s_fw[warp] = tot_t;
         __syncthreads();
         if (tid == 0) {
             float tot = 0.0f;
@@ -291,13 +351,20 @@ __global__ void __launch_bounds__(EXACT ? kBuildThreads : kRefineThreads)
     {
         uint32_t mine = 0;
         bool bad = EXACT && isnan(split);
-        for (uint32_t p = s + tid; p < e; p += T) {
-            float v = col[p];
-            mine += v < split ? 1u : 0u;
-            if (EXACT) bad |= isnan(v);
-        }
+        for (uint32_t b = s + tid; b < e; b += T * U) {
+            float v[U];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(kFull, mine, o);
+            for (int u = 0; u < U; ++u) {
+                const uint32_t p = b + u * T;
+                v[u] = p < e ? col[p] : split;  // split: neither < split nor NaN
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                mine += v[u] < split ? 1u : 0u;
+                if (EXACT) bad |= isnan(v[u]);
+            }
+        }
+        mine = __reduce_add_sync(kFull, mine);
         const bool wbad = __any_sync(kFull, bad);
         if (lane == 0) {
             s_w[warp] = mine;
@@ -321,60 +388,115 @@ __global__ void __launch_bounds__(EXACT ? kBuildThreads : kRefineThreads)
     const bool halve = !EXACT && (L == 0 || L == cntn || s_degenerate);
 
     // 4. partition: the k-th element >= split in [s, s+L) trades places with the
-    //    k-th element < split counted from the right end of [s+L, e)
+    //    k-th element < split counted from the right end of [s+L, e).  Right
+    //    side index i <-> position e-1-i, left side index i <-> position s+i;
+    //    each warp ranks a contiguous segment of each side.
     if (!halve) {
+        const uint32_t rlen = cntn - L;
+        const uint32_t lt = (1u << lane) - 1u;
+        uint32_t r0, r1, l0, l1;
+        warp_segment(rlen, r0, r1);
+        warp_segment(L, l0, l1);
+        uint32_t cr = 0, cl = 0;
+        for (uint32_t b = r0 + lane; b < r1; b += 32 * U) {
+            float v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t i = b + 32 * u;
+                v[u] = i < r1 ? col[e - 1 - i] : split;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) cr += v[u] < split ? 1u : 0u;
+        }
+        for (uint32_t b = l0 + lane; b < l1; b += 32 * U) {
+            float v[U];
+            bool in[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t i = b + 32 * u;
+                in[u] = i < l1;
+                v[u] = in[u] ? col[s + i] : split;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) cl += in[u] && !(v[u] < split) ? 1u : 0u;
+        }
+        cr = __reduce_add_sync(kFull, cr);
+        cl = __reduce_add_sync(kFull, cl);
+        uint32_t orr, ol, tr, tl;
+        warp_offsets2(cr, cl, s_w2, orr, ol, tr, tl);
+        // right side: the rank-k element < split goes to sel[s + k]
         {
-            uint32_t running = 0;
-            const uint32_t rlen = e - (s + L);
-            int par = 0;
-            for (uint32_t c = 0; c < rlen; c += T) {
-                const uint32_t i = c + tid;
-                bool f = false;
-                uint32_t p = 0;
-                if (i < rlen) {
-                    p = e - 1 - i;
-                    f = col[p] < split;
+            uint32_t run = orr;
+            for (uint32_t b = r0; b < r1; b += 32 * U) {
+                bool f[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const uint32_t i = b + 32 * u + lane;
+                    f[u] = i < r1 && col[e - 1 - i] < split;
                 }
-                uint32_t total;
-                uint32_t r = block_rank(f, s_w, par, total);
-                par ^= 1;
-                if (f) a.sel[s + running + r] = p;
-                running += total;
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const uint32_t m = __ballot_sync(kFull, f[u]);
+                    if (f[u]) a.sel[s + run + __popc(m & lt)] = e - 1 - (b + 32 * u + lane);
+                    run += __popc(m);
+                }
             }
         }
         __syncthreads();
+        // left side: the rank-k element >= split swaps with sel[s + k]
         {
-            uint32_t running = 0;
-            int par = 0;
-            for (uint32_t c = 0; c < L; c += T) {
-                const uint32_t i = c + tid;
-                bool f = false;
-                uint32_t p = 0;
-                if (i < L) {
-                    p = s + i;
-                    f = !(col[p] < split);
-                }
-                uint32_t total;
-                uint32_t r = block_rank(f, s_w, par, total);
-                par ^= 1;
-                if (f) {
-                    const uint32_t q = a.sel[s + running + r];
-                    if (q >= s + L && q < e) {
+            uint32_t run = ol;
+            for (uint32_t b = l0; b < l1; b += 32 * U) {
+                bool f[U];
+                uint32_t rk[U], q[U];
 #pragma unroll
-                        for (int d = 0; d < D; ++d) {
-                            float* cd = a.X + (uint64_t)d * n;
-                            float u = cd[p], v = cd[q];
-                            cd[p] = v;
-                            cd[q] = u;
-                        }
-                        uint32_t ip = a.tag[p], iq = a.tag[q];
-                        a.tag[p] = iq;
-                        a.tag[q] = ip;
-                    } else {  // unreachable: both sides count the same predicate
+                for (int u = 0; u < U; ++u) {
+                    const uint32_t i = b + 32 * u + lane;
+                    f[u] = i < l1 && !(col[s + i] < split);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const uint32_t m = __ballot_sync(kFull, f[u]);
+                    rk[u] = run + __popc(m & lt);
+                    run += __popc(m);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    q[u] = f[u] ? a.sel[s + rk[u]] : 0u;
+                    if (f[u] && !(q[u] >= s + L && q[u] < e)) {  // unreachable: both sides count the same predicate
                         atomicOr(a.err, kErrBadIndex);
+                        f[u] = false;
                     }
                 }
-                running += total;
+                // pairs are disjoint: every load before any store
+                float xp[U][D], xq[U][D];
+                uint32_t tp[U], tq[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (f[u]) {
+                        const uint32_t p = s + b + 32 * u + lane;
+#pragma unroll
+                        for (int d = 0; d < D; ++d) {
+                            xp[u][d] = a.X[(uint64_t)d * n + p];
+                            xq[u][d] = a.X[(uint64_t)d * n + q[u]];
+                        }
+                        tp[u] = a.tag[p];
+                        tq[u] = a.tag[q[u]];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (f[u]) {
+                        const uint32_t p = s + b + 32 * u + lane;
+#pragma unroll
+                        for (int d = 0; d < D; ++d) {
+                            a.X[(uint64_t)d * n + p] = xq[u][d];
+                            a.X[(uint64_t)d * n + q[u]] = xp[u][d];
+                        }
+                        a.tag[p] = tq[u];
+                        a.tag[q[u]] = tp[u];
+                    }
+                }
             }
         }
     }
@@ -1374,7 +1496,7 @@ int build_clouds(const CloudSet& cs, cudaStream_t stream, Scratch& sc, Built& ou
         b.cnt_cur = level_cnt + j;
         b.cnt_next = level_cnt + j + 1;
         stats_count_launch();
-        split_kernel<D, true><<<(unsigned)bound, kBuildThreads, 0, stream>>>(b, 0);
+        split_kernel<D, true, kBuildThreads><<<(unsigned)bound, kBuildThreads, 0, stream>>>(b, 0);
         FPSGPU_CUDA_TRY(cudaGetLastError());
         std::swap(b.cur, b.next);
     }
@@ -1393,6 +1515,12 @@ int build_clouds(const CloudSet& cs, cudaStream_t stream, Scratch& sc, Built& ou
     if (build_only) return FPSGPU_OK;
 
     // refinement phase
+    int sms = 0;
+    {
+        int dev = 0;
+        FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
+        FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    }
     uint32_t* rcnt = level_cnt + levels + 1;
     b.cnt_cur = rcnt;
     stats_count_launch();
@@ -1411,7 +1539,12 @@ int build_clouds(const CloudSet& cs, cudaStream_t stream, Scratch& sc, Built& ou
         b.cnt_next = rcnt + j + 1;
         const int last = j + 1 == refine_levels;
         stats_count_launch();
-        split_kernel<D, false><<<(unsigned)rbound, kRefineThreads, 0, stream>>>(b, last);
+        // few nodes (the top levels of a large vanilla cloud): wide CTAs, so
+        // that a node of millions of points streams through one SM fast
+        if (rbound <= (uint64_t)2 * std::max(1, sms))
+            split_kernel<D, false, kBuildThreads><<<(unsigned)rbound, kBuildThreads, 0, stream>>>(b, last);
+        else
+            split_kernel<D, false, kRefineThreads><<<(unsigned)rbound, kRefineThreads, 0, stream>>>(b, last);
         FPSGPU_CUDA_TRY(cudaGetLastError());
         std::swap(b.cur, b.next);
         rbound = std::min<uint64_t>(2 * rbound, rcap);
