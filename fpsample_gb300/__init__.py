@@ -33,6 +33,7 @@ try:
         __version__,
         _bucket_fps_kdline_sampling,
         _bucket_fps_kdline_sampling_batch,
+        _bucket_fps_kdline_sampling_batch_list,
         _bucket_fps_kdtree_sampling,
         _fps_npdu_kdtree_sampling,
         _fps_npdu_sampling,
@@ -154,11 +155,10 @@ def bucket_fps_kdline_sampling_batch(pcs, n_samples, h, start_idx=0):
         assert hh >= 1, "h should be >= 1"
         assert 2**hh <= n_pts, "2**h should be <= n_pts"
         assert 0 <= s < n_pts, "0 <= start_idx < n_pts"
-    sizes = np.array([np.asarray(p).shape[0] for p in pcs], dtype=np.uint64)
-    offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
-    pts = np.ascontiguousarray(np.concatenate([np.asarray(p, dtype=np.float32) for p in pcs]))
-    out = _bucket_fps_kdline_sampling_batch(pts, offsets, np.array(ks, np.uint64),
-                                            np.array(hs, np.uint64), np.array(ss, np.uint64))
+    # one buffer per cloud goes to the library as is: no host-side concatenation
+    clouds = [np.ascontiguousarray(p, dtype=np.float32) for p in pcs]
+    out = _bucket_fps_kdline_sampling_batch_list(clouds, np.array(ks, np.uint64),
+                                                 np.array(hs, np.uint64), np.array(ss, np.uint64))
     bounds = np.concatenate([[0], np.cumsum(ks)])
     return [out[bounds[i]:bounds[i + 1]] for i in range(m)]
 

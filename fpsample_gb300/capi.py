@@ -31,6 +31,8 @@ SIGNATURES = {
     "fpsgpu_fps_device_noalloc": (ctypes.c_int, [_vp, _sz, _sz, _sz, _szp, _sz, _vp, _vp, _vp]),
     "fpsgpu_kdline_build": (ctypes.c_int, [_f32p, _sz, _sz, _sz, _u64p, _u64p, _szp]),
     "fpsgpu_kdline_batch": (ctypes.c_int, [_f32p, _szp, _sz, _sz, _szp, _szp, _szp, _szp]),
+    "fpsgpu_kdline_batch_list": (ctypes.c_int, [ctypes.POINTER(_f32p), _szp, _sz, _sz, _szp, _szp,
+                                                _szp, _szp]),
     "fpsgpu_kdline_batch_device": (ctypes.c_int, [_vp, _szp, _sz, _sz, _szp, _szp, _szp, _vp, _vp]),
     "fpsgpu_server_create": (ctypes.c_int, [_sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)]),
     "fpsgpu_server_submit": (ctypes.c_int, [_vp, _f32p, _sz, _sz, _sz, _sz, _sz, _szp, _u64p]),
@@ -249,6 +251,25 @@ def kdline_batch(pcs, n_samples, heights, starts):
     _check("fpsgpu_kdline_batch", rc)
     b = np.concatenate([[0], np.cumsum(ks)]).astype(np.int64)
     return [out[b[i]:b[i + 1]] for i in range(len(pcs))]
+
+
+def kdline_batch_list(pcs, n_samples, heights, starts):
+    """Host-buffer batched QuickFPS with one buffer per cloud (no concatenation)
+    through the C ABI; list of uint64 arrays."""
+    clouds = [np.ascontiguousarray(p, np.float32) for p in pcs]
+    ptrs = (_f32p * max(1, len(clouds)))(*[c.ctypes.data_as(_f32p) for c in clouds])
+    npts = np.asarray([c.shape[0] for c in clouds], np.uint64)
+    dim = clouds[0].shape[1] if clouds else 3
+    ks = np.asarray(n_samples, np.uint64)
+    out = np.zeros(max(1, int(ks.sum())), np.uint64)
+    hs = np.asarray(heights, np.uint64)
+    ss = np.asarray(starts, np.uint64)
+    rc = lib().fpsgpu_kdline_batch_list(ptrs, npts.ctypes.data_as(_szp), len(clouds), dim,
+                                        ks.ctypes.data_as(_szp), ss.ctypes.data_as(_szp),
+                                        hs.ctypes.data_as(_szp), out.ctypes.data_as(_szp))
+    _check("fpsgpu_kdline_batch_list", rc)
+    b = np.concatenate([[0], np.cumsum(ks)]).astype(np.int64)
+    return [out[b[i]:b[i + 1]] for i in range(len(clouds))]
 
 
 def kdline_batch_device(points_ptr: int, offsets, dim: int, n_samples, heights, starts,

@@ -142,6 +142,15 @@ int cluster_size_for_batch() {
     return v;
 }
 
+// True when FPSGPU_CLUSTER_SIZE fixes the cluster size.  Otherwise a call whose
+// clustered clouds all fit the GPU at 16 CTAs each takes 16: the SMs would sit
+// idle anyway, and a 16-CTA cluster samples a 1M-point cloud about 4% faster
+// than an 8-CTA one (fewer pieces per CTA; the exchange costs the same).
+bool cluster_size_fixed() {
+    static const bool v = std::getenv("FPSGPU_CLUSTER_SIZE") != nullptr;
+    return v;
+}
+
 // FPSGPU_CLUSTER_MIN_PIECES: clouds with at least this many pieces run on a
 // cluster even when one CTA could hold them (0, the default: only clouds that
 // need it).  A tuning knob for batches whose largest clouds set the makespan.
@@ -403,6 +412,38 @@ int fp_mode() {
     return g_fp_mode;
 }
 }  // namespace
+
+// Whether kernels on device `dev` may read pageable host memory through the
+// host's page tables (hardware-coherent hosts such as Grace): then a kernel can
+// gather host buffers itself.  Queried once per device.
+int reads_host_page_tables(int dev, int* out) {
+    static std::mutex mu;
+    static std::vector<int> cache;  // -1: not queried yet
+    std::lock_guard<std::mutex> lk(mu);
+    if ((int)cache.size() <= dev) cache.resize(dev + 1, -1);
+    if (cache[dev] < 0) {
+        int pageable = 0, tables = 0;
+        FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
+        FPSGPU_CUDA_TRY(
+            cudaDeviceGetAttribute(&tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
+        cache[dev] = pageable && tables ? 1 : 0;
+    }
+    *out = cache[dev];
+    return FPSGPU_OK;
+}
+
+// dst[foff[c] + i] = src[c][i]: every cloud from its own host buffer into one
+// device buffer (y: clouds, x: chunks of a cloud).
+__global__ void gather_host_clouds(const float* const* src, const uint64_t* foff, uint32_t n_clouds,
+                                   float* __restrict__ dst) {
+    for (uint32_t c = blockIdx.y; c < n_clouds; c += gridDim.y) {
+        const float* sc = src[c];
+        const uint64_t b = foff[c], m = foff[c + 1] - b;
+        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+             i += (uint64_t)gridDim.x * blockDim.x)
+            dst[b + i] = sc[i];
+    }
+}
 
 }  // namespace fpsgpu
 
@@ -805,6 +846,67 @@ int fpsgpu_kdline_batch(const float* raw_data, const size_t* offsets, size_t n_c
     FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_pts, raw_data, n * dim * sizeof(float),
                                     cudaMemcpyHostToDevice, ctx.stream));
     if ((rc = fpsgpu_kdline_batch_device(d_pts, offsets, n_clouds, dim, n_samples, start_idx,
+                                         height, d_out, ctx.stream)))
+        return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(sampled_point_indices, d_out, ktot * sizeof(uint64_t),
+                                    cudaMemcpyDeviceToHost, ctx.stream));
+    FPSGPU_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
+    return FPSGPU_OK;
+}
+
+int fpsgpu_kdline_batch_list(const float* const* clouds, const size_t* n_points, size_t n_clouds,
+                             size_t dim, const size_t* n_samples, const size_t* start_idx,
+                             const size_t* height, size_t* sampled_point_indices) {
+    clear_error();
+    if (n_clouds == 0) return FPSGPU_OK;
+    if (!clouds || !n_points || !n_samples) return set_error(FPSGPU_ERR_ARG, "null argument");
+    if (dim == 0 || dim > 8) return set_error(FPSGPU_ERR_DIM, "dim must be in [1, 8], got %zu", dim);
+    std::vector<size_t> off(n_clouds + 1, 0);
+    std::vector<uint64_t> foff(n_clouds + 1, 0);  // in floats
+    size_t ktot = 0, max_f = 0;
+    for (size_t c = 0; c < n_clouds; ++c) {
+        if (n_points[c] > 0 && clouds[c] == nullptr)
+            return set_error(FPSGPU_ERR_ARG, "cloud %zu has points but a null buffer", c);
+        off[c + 1] = off[c] + n_points[c];
+        foff[c + 1] = foff[c] + (uint64_t)n_points[c] * dim;
+        max_f = std::max<size_t>(max_f, n_points[c] * dim);
+        ktot += n_samples[c];
+    }
+    DevCtx ctx;
+    int rc;
+    if ((rc = current_ctx(&ctx))) return rc;
+    Scratch sc(ctx.stream);
+    const size_t n = off[n_clouds];
+    float* d_pts;
+    uint64_t* d_out;
+    if ((rc = sc.alloc(&d_pts, n * dim))) return rc;
+    if ((rc = sc.alloc(&d_out, ktot))) return rc;
+    int host_tables = 0;
+    if ((rc = reads_host_page_tables(ctx.device, &host_tables))) return rc;
+    if (host_tables) {
+        // one kernel reads every cloud from its own host buffer
+        const float** d_src;
+        uint64_t* d_foff;
+        if ((rc = sc.alloc(&d_src, n_clouds))) return rc;
+        if ((rc = sc.alloc(&d_foff, n_clouds + 1))) return rc;
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_src, clouds, n_clouds * sizeof(float*), cudaMemcpyHostToDevice,
+                                        ctx.stream));
+        FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_foff, foff.data(), (n_clouds + 1) * sizeof(uint64_t),
+                                        cudaMemcpyHostToDevice, ctx.stream));
+        const unsigned gx = (unsigned)std::min<size_t>((max_f + 2047) / 2048, 512);
+        const unsigned gy = (unsigned)std::min<size_t>(n_clouds, 65535);
+        stats_count_launch();
+        gather_host_clouds<<<dim3(std::max(1u, gx), gy), 256, 0, ctx.stream>>>(d_src, d_foff,
+                                                                            (uint32_t)n_clouds, d_pts);
+        FPSGPU_CUDA_TRY(cudaGetLastError());
+    } else {
+        for (size_t c = 0; c < n_clouds; ++c)
+            if (n_points[c] > 0)
+                FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_pts + foff[c], clouds[c],
+                                                n_points[c] * dim * sizeof(float),
+                                                cudaMemcpyHostToDevice, ctx.stream));
+    }
+    if ((rc = fpsgpu_kdline_batch_device(d_pts, off.data(), n_clouds, dim, n_samples, start_idx,
                                          height, d_out, ctx.stream)))
         return rc;
     FPSGPU_CUDA_TRY(cudaMemcpyAsync(sampled_point_indices, d_out, ktot * sizeof(uint64_t),

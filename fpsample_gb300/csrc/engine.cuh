@@ -2081,8 +2081,9 @@ struct BatchCall {
     bool tie_last = false;            // bucket_fps_kdtree
     float* d_out_pts = nullptr;       // null, or [sum k][D], cloud c at row out_off[c]
     // smallest cluster for clouds that need one (0: the latency default,
-    // cluster_size_for_batch(); 1: just as many CTAs as the pieces need, which
-    // leaves more SMs to other work, e.g. in the server)
+    // cluster_size_for_batch(), or 16 when every cloud of the call fits the
+    // GPU at once with that size; 1: just as many CTAs as the pieces need,
+    // which leaves more SMs to other work, e.g. in the server)
     int min_cluster = 0;
 };
 
@@ -2167,6 +2168,12 @@ int run_batch(const BatchCall& bc) {
                                 : (const void*)batch_sample<D, FMA, false, true>;
     const size_t cl_smem = batch_smem_bytes(D, cap_max, 0);
     int maxc = 0;
+    if (!clustered.empty() && bc.min_cluster == 0 && !cluster_size_fixed() && cl < kMaxCluster &&
+        small.size() + clustered.size() * kMaxCluster <= (size_t)bc.sms) {
+        int m16 = 0;
+        if ((rc = cluster_capacity(cl_kern, kMaxCluster, batch_threads(D), cl_smem, &m16))) return rc;
+        if ((size_t)m16 >= clustered.size()) cl = kMaxCluster;
+    }
     if (!clustered.empty()) {
         if ((rc = cluster_capacity(cl_kern, cl, batch_threads(D), cl_smem, &maxc))) return rc;
         if (maxc < 1) {  // no such cluster on this device: the other samplers take them

@@ -162,6 +162,7 @@ int allow_cluster16(const void* func);
 
 // thread-block cluster launches (batched engine's cluster sampler)
 int cluster_size_for_batch();
+bool cluster_size_fixed();
 uint32_t cluster_min_pieces();
 int cluster_capacity(const void* func, int cl, int block, size_t smem, int* out);
 int launch_clustered(const void* func, int items, int cl, int block, void** args, size_t smem,

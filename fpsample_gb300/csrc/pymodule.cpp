@@ -230,6 +230,48 @@ Indices bucket_fps_kdline_sampling_batch(FloatRows points, Indices offsets, Indi
     return out;
 }
 
+// Batched QuickFPS over a list of clouds, each its own (n_i, D) float32 array:
+// no concatenation on the host.  Same checks and result layout as
+// bucket_fps_kdline_sampling_batch.
+Indices bucket_fps_kdline_sampling_batch_list(py::list pcs, Indices n_samples, Indices heights,
+                                              Indices starts) {
+    const ssize_t C = (ssize_t)pcs.size();
+    if (n_samples.size() != C || heights.size() != C || starts.size() != C)
+        throw py::value_error("n_samples, heights and starts need one entry per cloud");
+    std::vector<FloatRows> arrs;
+    arrs.reserve(C);
+    std::vector<const float*> ptrs(C);
+    std::vector<size_t> npts(C);
+    size_t total = 0, dim = 0;
+    for (ssize_t c = 0; c < C; ++c) {
+        arrs.push_back(FloatRows::ensure(pcs[c]));
+        const FloatRows& a = arrs.back();
+        if (!a || a.ndim() != 2) throw py::value_error("every cloud must be a 2D float32 array");
+        if (c == 0) dim = (size_t)a.shape(1);
+        if ((size_t)a.shape(1) != dim) throw py::value_error("all clouds must have the same dimension");
+        const size_t nc = (size_t)a.shape(0);
+        const size_t k = n_samples.data()[c];
+        if (nc == 0) throw py::value_error("empty cloud in the batch");
+        if (starts.data()[c] >= nc) throw py::value_error("start_idx out of range");
+        if (k == 0 || k > nc) throw py::value_error("n_samples must be in [1, num_points]");
+        if (heights.data()[c] == 0) throw py::value_error("height must be >= 1");
+        ptrs[c] = a.data();
+        npts[c] = nc;
+        total += k;
+    }
+    Indices out(total);
+    if (C == 0) return out;
+    int rc;
+    size_t* out_ptr = static_cast<size_t*>(out.mutable_data());
+    {
+        py::gil_scoped_release nogil;
+        rc = fpsgpu_kdline_batch_list(ptrs.data(), npts.data(), (size_t)C, dim, n_samples.data(),
+                                      starts.data(), heights.data(), out_ptr);
+    }
+    if (rc != 0) raise_gpu_failure("fpsgpu_kdline_batch_list", rc);
+    return out;
+}
+
 [[noreturn]] void not_in_gpu_build(const char* name) {
     PyErr_SetString(PyExc_NotImplementedError,
                     (std::string(name) +
@@ -330,6 +372,9 @@ PYBIND11_MODULE(_fpsample, m) {
     m.attr("ALGO_KDTREE") = FPSGPU_ALGO_KDTREE;
     m.def("_bucket_fps_kdline_sampling_batch", &bucket_fps_kdline_sampling_batch,
           "many clouds in one GPU call: (points, offsets, n_samples, heights, starts) -> indices");
+    m.def("_bucket_fps_kdline_sampling_batch_list", &bucket_fps_kdline_sampling_batch_list,
+          "many clouds in one GPU call, one array per cloud: (clouds, n_samples, heights, starts) "
+          "-> indices");
     m.def("_kdline_build", &kdline_build,
           "kd-line tree build alone: (perm uint64[N], bucket_starts uint64[B])");
     m.def("_get_fp_mode", &get_fp_mode, "current floating-point mode: 'nofma' or 'fma'");

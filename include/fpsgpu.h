@@ -135,6 +135,22 @@ int fpsgpu_kdline_batch(const float *raw_data, const size_t *offsets, size_t n_c
                         size_t dim, const size_t *n_samples, const size_t *start_idx,
                         const size_t *height, size_t *sampled_point_indices);
 
+/*
+ * fpsgpu_kdline_batch with every cloud in its own host buffer: cloud c is
+ * clouds[c], row-major n_points[c] x dim float.  The caller does not have to
+ * concatenate the clouds first (for 256 clouds of 83 MB in all that copy cost
+ * more host time than moving the data to the GPU).  Where the GPU reads
+ * pageable host memory through the host's page tables (Grace), one kernel
+ * gathers the clouds straight from the buffers; elsewhere each cloud is one
+ * host-to-device copy.  Same checks, codes and results as fpsgpu_kdline_batch;
+ * the reference's per-cloud equivalent is src/wrapper.hpp:118-132 called in a
+ * loop.  Host buffers; synchronous.
+ */
+int fpsgpu_kdline_batch_list(const float *const *clouds, const size_t *n_points,
+                             size_t n_clouds, size_t dim, const size_t *n_samples,
+                             const size_t *start_idx, const size_t *height,
+                             size_t *sampled_point_indices);
+
 /* Device-buffer form of fpsgpu_kdline_batch: d_points and d_out are device
    pointers, the per-cloud arrays are HOST arrays; stream as above. */
 int fpsgpu_kdline_batch_device(const float *d_points, const size_t *h_offsets,

@@ -79,3 +79,23 @@ def test_vanilla_argument_checks_without_gpu():
                       out.ctypes.data_as(capi._szp))
     assert rc == 1
     assert "dim" in L.fpsgpu_last_error().decode()
+
+
+def test_batch_list_argument_checks_without_gpu():
+    """fpsgpu_kdline_batch_list rejects a bad dimension and a cloud with points
+    but no buffer before it touches the GPU; an empty batch succeeds."""
+    L = capi.lib()
+    a = np.zeros((10, 3), np.float32)
+    ptrs = (capi._f32p * 2)(a.ctypes.data_as(capi._f32p), capi._f32p())
+    npts = np.array([10, 10], np.uint64)
+    ks = np.array([2, 2], np.uint64)
+    hs = np.array([1, 1], np.uint64)
+    ss = np.array([0, 0], np.uint64)
+    out = np.zeros(4, np.uint64)
+    args = (npts.ctypes.data_as(capi._szp),)
+    rest = (ks.ctypes.data_as(capi._szp), ss.ctypes.data_as(capi._szp),
+            hs.ctypes.data_as(capi._szp), out.ctypes.data_as(capi._szp))
+    assert L.fpsgpu_kdline_batch_list(ptrs, *args, 2, 9, *rest) == 1
+    assert L.fpsgpu_kdline_batch_list(ptrs, *args, 2, 3, *rest) == 3
+    assert "null buffer" in L.fpsgpu_last_error().decode()
+    assert L.fpsgpu_kdline_batch_list(ptrs, *args, 0, 3, *rest) == 0

@@ -347,6 +347,21 @@ def test_batch_identical_to_one_call_per_cloud():
         np.testing.assert_array_equal(g, fps.bucket_fps_kdline_sampling(p, k, h, s))
 
 
+def test_batch_list_form_equals_contiguous_form():
+    """One host buffer per cloud (fpsgpu_kdline_batch_list, the Python batch API's
+    path) gives the same indices as the concatenated buffer (fpsgpu_kdline_batch),
+    including clouds that are strided or float64 on the Python side."""
+    clouds, ks, hs, ss = _batch_clouds(12, 30, 200, 40000)
+    clouds[3] = np.asfortranarray(clouds[3])
+    clouds[5] = clouds[5].astype(np.float64)
+    want = capi.kdline_batch(clouds, ks, hs, ss)
+    got_c = capi.kdline_batch_list(clouds, ks, hs, ss)
+    got_py = fps.bucket_fps_kdline_sampling_batch(clouds, ks, hs, ss)
+    for w, a, b in zip(want, got_c, got_py):
+        np.testing.assert_array_equal(a, w)
+        np.testing.assert_array_equal(b, w)
+
+
 def test_batched_workload_sample_vs_oracle():
     """The bench's 256-cloud workload: every 16th cloud checked against the oracle."""
     clouds = W.batched_clouds(seed=W.SEEDS["batched-256"])
