@@ -1023,6 +1023,7 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
         // my pieces: slot j holds local piece j * T + lane * nwarps + warp,
         // which is the cloud's piece local * C + rank
         const uint32_t nmine = np > rank ? (np - rank + C - 1) / C : 0u;
+        const uint32_t ns = (nmine + T - 1) / T;  // slots in use by some thread
         float lo[batch_slots(D)][D], hi[batch_slots(D)][D];
         uint64_t key[batch_slots(D)];
         uint32_t myq[batch_slots(D)];
@@ -1084,15 +1085,18 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
             uint32_t dm = 0;  // my dirty slots, one bit each
 #pragma unroll
             for (int j = 0; j < batch_slots(D); ++j) {
-                const bool dj = first ? myq[j] < nmine
-                                      : box_bound<D, FMA>(lo[j], hi[j], r) < key_dist(key[j]);
-                dm |= (uint32_t)dj << j;
+                if ((uint32_t)j < ns) {  // CTA-uniform: slots no thread uses are not tested
+                    const bool dj = first ? myq[j] < nmine
+                                          : box_bound<D, FMA>(lo[j], hi[j], r) < key_dist(key[j]);
+                    dm |= (uint32_t)dj << j;
+                }
             }
             // keys change only in dirty slots: the lane and warp maxima are
             // recomputed only where something was dirty
             if (__any_sync(kFull, dm != 0)) {
 #pragma unroll
                 for (int j = 0; j < batch_slots(D); ++j) {
+                    if ((uint32_t)j >= ns) break;
                     uint32_t m = __ballot_sync(kFull, (dm >> j) & 1u);
                     while (m) {
                         const int l = __ffs(m) - 1;
