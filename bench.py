@@ -53,6 +53,10 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# 32 hardware work queues (default 8) before anything touches CUDA: the request
+# server's worker streams must not share queues (a small batch would wait
+# behind a large batch's kernel in the same queue)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "clouds/sec"
 UNIT = "clouds/s"

@@ -23,9 +23,16 @@ default); ``set_fp_mode("fma" | "nofma")`` selects which one to match (default
 """
 from __future__ import annotations
 
+import os
 from typing import List, Optional, Union
 
 import numpy as np
+
+# More hardware work queues than the default 8, so that kernels on different
+# streams (request-server workers, the batched engine's side stream) never wait
+# for each other by sharing a queue.  Read when the process first uses CUDA, so
+# it only takes effect if this package is imported before that.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 try:
     from ._fpsample import (

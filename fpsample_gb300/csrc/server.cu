@@ -13,7 +13,12 @@
 //
 // Size classes keep small requests from waiting behind very large ones:
 // requests of at most kSmallPoints points go to the "small" workers, the rest
-// to the "large" workers.
+// to the "large" workers, and a batch only gathers requests of similar sample
+// counts.  Each worker has its own stream; the streams only run side by side if
+// the device has enough hardware work queues (CUDA_DEVICE_MAX_CONNECTIONS, 8
+// unless set before the process first uses CUDA; the Python package sets 32),
+// otherwise a small batch can wait behind a large batch's kernel that shares
+// its queue.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -106,15 +111,31 @@ struct Server {
                 std::unique_lock<std::mutex> lk(mu);
                 cv_work.wait(lk, [&] { return stopping || !pending[cls].empty(); });
                 if (stopping && pending[cls].empty()) break;
-                // admit in arrival order while the memory budget allows; a
-                // request larger than the whole budget still runs alone
-                while (!pending[cls].empty() && batch.size() < kMaxBatch) {
-                    Request* r = pending[cls].front();
-                    if (!batch.empty() && r->dim != batch[0]->dim) break;
-                    if (in_use + bytes + r->bytes > budget && !(in_use == 0 && batch.empty())) break;
-                    pending[cls].pop_front();
-                    bytes += r->bytes;
-                    batch.push_back(r);
+                // the oldest waiting request opens the batch (a request larger
+                // than the whole budget still runs alone once nothing else is
+                // on the device); others join, in arrival order, while the
+                // memory budget allows and only if their sample count is
+                // within a factor of two of its own: a batch completes with its
+                // longest cloud, so no request waits long for a much longer one
+                {
+                    Request* r0 = pending[cls].front();
+                    if (in_use + r0->bytes <= budget || in_use == 0) {
+                        pending[cls].pop_front();
+                        bytes += r0->bytes;
+                        batch.push_back(r0);
+                        for (auto it = pending[cls].begin();
+                             it != pending[cls].end() && batch.size() < kMaxBatch;) {
+                            Request* r = *it;
+                            if (r->dim == r0->dim && r->k <= 2 * r0->k && 2 * r->k >= r0->k &&
+                                in_use + bytes + r->bytes <= budget) {
+                                bytes += r->bytes;
+                                batch.push_back(r);
+                                it = pending[cls].erase(it);
+                            } else {
+                                ++it;
+                            }
+                        }
+                    }
                 }
                 if (batch.empty()) {  // nothing fits now: wait for memory to free up
                     cv_done.wait(lk);

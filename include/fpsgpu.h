@@ -161,11 +161,17 @@ int fpsgpu_kdline_batch_device(const float *d_points, const size_t *h_offsets,
 /*
  * Request server (no counterpart in the reference): bucket_fps_kdline as a
  * service with continuous batching.  Worker threads, one CUDA stream each,
- * repeatedly take every waiting request of their size class (at most 262144
- * points: "small" workers; larger: "large" workers) that fits in the
- * device-memory budget and run them as one batch; requests arriving meanwhile
- * go to the next free worker, so batches overlap on the GPU.  Every result is
- * identical to one bucket_fps_kdline call on that cloud.
+ * repeatedly take the oldest waiting request of their size class (at most
+ * 131072 points: "small" workers; larger: "large" workers) together with the
+ * other waiting requests whose sample counts are within a factor of two of
+ * its own, as far as the device-memory budget allows, and run them as one
+ * batch; requests arriving meanwhile go to the next free worker, so batches
+ * overlap on the GPU.  Every result is identical to one bucket_fps_kdline call
+ * on that cloud.  The workers' streams only run side by side if the process
+ * has enough hardware work queues: set CUDA_DEVICE_MAX_CONNECTIONS=32 before
+ * the process first uses CUDA (the default, 8, let a small batch wait behind
+ * a large batch's kernel: p99 latency of clouds up to 64K points 533 ms
+ * instead of 21 ms in one measurement).
  *   create : budget in bytes of device memory for admitted requests
  *   submit : host buffers; `points` and `sampled_point_indices` must stay valid
  *            until fpsgpu_server_wait returns for the ticket
