@@ -445,6 +445,30 @@ __global__ void gather_host_clouds(const float* const* src, const uint64_t* foff
     }
 }
 
+namespace {
+std::atomic<long long> g_alloc_budget{-1};
+}  // namespace
+
+bool scratch_alloc_refused() {
+    long long v = g_alloc_budget.load();
+    while (v >= 0) {
+        if (v == 0) return true;
+        if (g_alloc_budget.compare_exchange_weak(v, v - 1)) return false;
+    }
+    return false;
+}
+
+// Self-test of the grid exchange's bounded wait: ONE CTA runs exchange_leader
+// for a grid of two, so the record of CTA 1 never arrives; the leader must give
+// up after `limit` polls, set the error word and return.
+__global__ void selftest_exchange_timeout(uint64_t* slots, int* err, long long limit) {
+    if (threadIdx.x < 32) {
+        const float c[3] = {0.0f, 0.0f, 0.0f};
+        float w[3];
+        (void)exchange_leader<3>(slots, slots + 2 * leader_words<3>(), 2, 0u, 1ull, c, w, err, limit);
+    }
+}
+
 }  // namespace fpsgpu
 
 using namespace fpsgpu;
@@ -914,6 +938,27 @@ int fpsgpu_kdline_batch_list(const float* const* clouds, const size_t* n_points,
     FPSGPU_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
     return FPSGPU_OK;
 }
+
+int fpsgpu_selftest_exchange_timeout(void) {
+    clear_error();
+    DevCtx ctx;
+    int rc;
+    if ((rc = current_ctx(&ctx))) return rc;
+    Scratch sc(ctx.stream);
+    uint64_t* slots;
+    int* err;
+    const size_t nslots = 2 * leader_words<3>() + leader_words<3>();
+    if ((rc = sc.alloc(&slots, nslots))) return rc;
+    if ((rc = sc.alloc(&err, 1))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemsetAsync(slots, 0, nslots * sizeof(uint64_t), ctx.stream));
+    FPSGPU_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), ctx.stream));
+    stats_count_launch();
+    selftest_exchange_timeout<<<1, 32, 0, ctx.stream>>>(slots, err, 4096);
+    FPSGPU_CUDA_TRY(cudaGetLastError());
+    return check_device_error(err, ctx.stream);
+}
+
+void fpsgpu_debug_fail_allocations(long long after) { g_alloc_budget.store(after < 0 ? -1 : after); }
 
 int fpsgpu_kdline_build(const float* raw_data, size_t n_points, size_t dim, size_t height,
                         uint64_t* h_perm, uint64_t* h_bucket_start, size_t* n_buckets) {

@@ -355,11 +355,13 @@ __device__ __forceinline__ void ld_relaxed_gpu_v2(const uint64_t* p, uint64_t& a
 // t+1 only after every CTA has published round t+1, i.e. after every CTA has
 // read the round-t broadcast.  L2 traffic per round is O(G) (the gather plus
 // one record per CTA), not the O(G^2) of an all-to-all poll.
-// Every poll loop gives up after kSpinLimit rounds: err is set, 0 returned.
+// Every poll loop gives up after `limit` rounds (kSpinLimit unless a self-test
+// asks for fewer): err is set, 0 returned.
 template <int D>
 __device__ __forceinline__ uint64_t exchange_leader(uint64_t* slots, uint64_t* bcast, int G,
                                                     uint32_t round, uint64_t my_key,
-                                                    const float* my_c, float* win_c, int* err) {
+                                                    const float* my_c, float* win_c, int* err,
+                                                    long long limit = kSpinLimit) {
     constexpr int SW = leader_words<D>();
     constexpr int kPer = kMaxGridCoords / 32;
     const int lane = threadIdx.x & 31;
@@ -407,7 +409,7 @@ __device__ __forceinline__ uint64_t exchange_leader(uint64_t* slots, uint64_t* b
             for (int i = 0; i < kPer; ++i)
                 if (lane + 32 * i < G && !((done >> i) & 1u)) all = false;
             if (__all_sync(kFull, all)) break;
-            if (++spins > kSpinLimit) {
+            if (++spins > limit) {
                 ok = false;
                 break;
             }
@@ -441,7 +443,7 @@ __device__ __forceinline__ uint64_t exchange_leader(uint64_t* slots, uint64_t* b
 #pragma unroll
             for (int k = 0; k < 2 + D; ++k) good &= (uint32_t)(w[k] >> 32) == rt;
             if (good) break;
-            if (++spins > kSpinLimit) {
+            if (++spins > limit) {
                 ok = false;
                 break;
             }

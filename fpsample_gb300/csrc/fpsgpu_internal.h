@@ -44,6 +44,10 @@ int current_ctx(DevCtx* ctx);
 void set_thread_pool(cudaMemPool_t pool);
 cudaMemPool_t thread_pool();
 
+// Fault injection on the host (fpsgpu_debug_fail_allocations): the number of
+// stream-ordered scratch allocations that may still succeed, or -1 (off).
+bool scratch_alloc_refused();
+
 class Scratch {
    public:
     explicit Scratch(cudaStream_t s) : s_(s) {}
@@ -56,6 +60,8 @@ class Scratch {
     int alloc(T** out, size_t count) {
         void* p = nullptr;
         size_t bytes = count ? count * sizeof(T) : sizeof(T);
+        if (scratch_alloc_refused())
+            return set_error(FPSGPU_ERR_CUDA, "cudaMallocAsync(%zu bytes) refused (injected fault)", bytes);
         cudaMemPool_t pool = thread_pool();
         cudaError_t e = pool ? cudaMallocFromPoolAsync(&p, bytes, pool, s_)
                              : cudaMallocAsync(&p, bytes, s_);

@@ -231,6 +231,22 @@ void fpsgpu_stats_timing(int enable);
 /* message describing the last failure on the calling thread ("" if none) */
 const char *fpsgpu_last_error(void);
 
+/*
+ * Failure handling checks (no counterpart in the reference, whose C ABI only
+ * returns argument codes).  Every wait of the multi-CTA samplers on another
+ * CTA is bounded: past its limit the kernel sets an error word and exits, and
+ * the call returns FPSGPU_ERR_DEVICE instead of hanging.
+ *   fpsgpu_selftest_exchange_timeout: runs the samplers' grid exchange on one
+ *     CTA for a grid of two, so the partner never arrives, with a limit of 4096
+ *     polls; returns FPSGPU_ERR_DEVICE when the bounded wait works.  The GPU
+ *     stays usable afterwards.
+ *   fpsgpu_debug_fail_allocations: host-side fault injection.  After `after`
+ *     more successful scratch allocations (any thread) every scratch
+ *     allocation fails with FPSGPU_ERR_CUDA, until called with -1.
+ */
+int fpsgpu_selftest_exchange_timeout(void);
+void fpsgpu_debug_fail_allocations(long long after);
+
 /* library version string */
 const char *fpsgpu_version(void);
 
