@@ -38,12 +38,19 @@
 //      every piece holds at most kPiece points.  Pieces tile the storage order.
 //   3. exact bounding box of every piece.
 //
-// Sampling (fps_sample): a persistent cooperative grid; every warp owns a run
-// of pieces and keeps each piece's max key (running distance, tag).  For a new
-// reference point r, a piece whose box_bound(r) >= its max cannot change (see
-// box_bound) and is skipped; other pieces recompute their points.  The grid
-// argmax runs through exchange_max; the winner's coordinates come from Xref by
-// tag.
+// Sampling.  Every sampler keeps each piece's max key (running distance, tag)
+// and box; for a new reference point r, a piece whose box_bound(r) >= its max
+// cannot change (see box_bound) and is skipped; other pieces recompute their
+// points.  Samplers differ in who holds the pieces and how the argmax is
+// combined:
+//   * batch_sample<CL=false>: one CTA per cloud from a persistent queue,
+//     piece records in registers, one __syncthreads per sample;
+//   * batch_sample<CL=true>: one thread-block cluster per cloud, the CTAs'
+//     maxima exchanged through distributed shared memory (st.async + mbarrier);
+//   * grid_sample_reg / grid_sample_smem / fps_sample: one cloud on a
+//     persistent cooperative grid, the grid-wide argmax through
+//     exchange_leader (which also delivers the winner's coordinates; fps_sample
+//     reads them from Xref by tag).
 #pragma once
 
 #include <algorithm>
@@ -1590,7 +1597,8 @@ inline int check_device_error(const int* d_err, cudaStream_t stream) {
 // pieces and keeps their points (coordinates, running distance, tag) and piece
 // records (max key, box, coordinates of the max) in shared memory for the
 // whole run.  One iteration = shared-memory work, one __syncthreads, and one
-// exchange_max_coords round trip that also delivers the next reference point.
+// exchange_leader round (the grid-wide argmax, which also delivers the winner's
+// coordinates: the next reference point).
 constexpr int kSmemThreads = 512;
 
 struct GridSmemArgs {

@@ -251,79 +251,8 @@ __device__ __forceinline__ uint64_t exchange_max(uint64_t* slots, int G, uint32_
     return best;
 }
 
-// Largest grid exchange_max_coords supports (5 slots per polling lane).
+// Largest grid exchange_leader supports (5 slots per polling lane).
 constexpr int kMaxGridCoords = 160;
-
-// exchange_max plus the coordinates of the winning point, in the same round
-// trip.  Each slot is 1 + D u64 words: the key (same validity/clearing
-// protocol as exchange_max) and one word per coordinate holding
-// (round + 1) << 32 | float bits.  A 64-bit word is written and read whole, so a
-// coordinate word carrying this round's tag holds this round's coordinate; a
-// poller therefore never needs a second, ordered load for the winner.
-template <int D>
-__device__ __forceinline__ uint64_t exchange_max_coords(uint64_t* slots, int G, uint32_t round,
-                                                        uint64_t my_key, const float* my_c,
-                                                        float* win_c, int* err) {
-    constexpr int kPer = kMaxGridCoords / 32;
-    constexpr int W = 1 + D;
-    const int lane = threadIdx.x & 31;
-    uint64_t* row = slots + (uint64_t)(round % 3u) * G * W;
-    const uint32_t rtag = round + 1u;
-    if (lane == 0) {
-        uint64_t* mine = row + (uint64_t)blockIdx.x * W;
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            st_relaxed_gpu(mine + 1 + d, ((uint64_t)rtag << 32) | __float_as_uint(my_c[d]));
-        st_release_gpu(mine, my_key | kKeyValid);
-    }
-    uint64_t best = 0;
-    float bc[D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) bc[d] = 0.0f;
-    unsigned done = 0;
-    long long spins = 0;
-    for (;;) {
-#pragma unroll
-        for (int i = 0; i < kPer; ++i) {
-            const int j = lane + 32 * i;
-            if (j < G && !((done >> i) & 1u)) {
-                const uint64_t* sl = row + (uint64_t)j * W;
-                const uint64_t k = ld_relaxed_gpu(sl);
-                uint64_t cw[D];
-#pragma unroll
-                for (int d = 0; d < D; ++d) cw[d] = ld_relaxed_gpu(sl + 1 + d);
-                bool ok = k != 0;
-#pragma unroll
-                for (int d = 0; d < D; ++d) ok &= (uint32_t)(cw[d] >> 32) == rtag;
-                if (ok) {
-                    done |= 1u << i;
-                    if (k > best) {
-                        best = k;
-#pragma unroll
-                        for (int d = 0; d < D; ++d) bc[d] = __uint_as_float((uint32_t)cw[d]);
-                    }
-                }
-            }
-        }
-        bool mine_done = true;
-#pragma unroll
-        for (int i = 0; i < kPer; ++i)
-            if (lane + 32 * i < G && !((done >> i) & 1u)) mine_done = false;
-        if (__all_sync(kFull, mine_done)) break;
-        if (++spins > kSpinLimit) {
-            if (lane == 0) atomicOr(err, kErrExchangeTimeout);
-            return 0;
-        }
-    }
-    fence_acq_rel_gpu();
-    const uint64_t g = warp_max_key(best);
-    const int owner = __ffs(__ballot_sync(kFull, best == g)) - 1;
-#pragma unroll
-    for (int d = 0; d < D; ++d) win_c[d] = __shfl_sync(kFull, bc[d], owner);
-    if (lane == 0)
-        st_relaxed_gpu(slots + (uint64_t)((round + 2u) % 3u) * G * W + (uint64_t)blockIdx.x * W, 0ull);
-    return g;
-}
 
 __device__ __forceinline__ uint64_t tagged(uint32_t tag, uint32_t payload) {
     return ((uint64_t)tag << 32) | payload;
