@@ -8,7 +8,8 @@
 * Host-side fault injection: fpsgpu_debug_fail_allocations refuses the N-th
   scratch allocation.  For every N up to the first one the call survives, the
   call must raise the reference's RuntimeError, and the next call must succeed
-  with the same indices as before.
+  with the same indices as before.  In the request server, a refused batch
+  fails its requests and the workers keep serving.
 """
 import numpy as np
 import pytest
@@ -67,3 +68,31 @@ def test_refused_allocations_fail_cleanly_and_the_next_call_recovers(algo):
     else:
         pytest.fail("the call never completed within 200 allocations")
     assert refused >= 3
+
+
+def test_request_server_fails_requests_cleanly_and_keeps_serving():
+    """A batch whose scratch allocation is refused fails its requests with
+    FPSGPU_ERR_CUDA; the server's workers carry on and later requests are
+    exact."""
+    from fpsample_gb300 import workloads as W
+
+    lib = capi.lib()
+    rng = np.random.default_rng(73)
+    reqs = []
+    for n in (5000, 12000, 30000):
+        p = W.sphere_cloud(rng, n)
+        reqs.append((p, n // 8, 7 if n >= 8192 else 5, int(rng.integers(0, n))))
+    want = [fps.bucket_fps_kdline_sampling(p, k, h, s) for p, k, h, s in reqs]
+    with capi.Server(1 << 30, small_workers=1, large_workers=1) as srv:
+        lib.fpsgpu_debug_fail_allocations(0)
+        try:
+            p, k, h, s = reqs[0]
+            t = srv.submit(p, k, h, s)
+            with pytest.raises(capi.FpsGpuError) as e:
+                srv.result(t)
+            assert e.value.code == 4
+        finally:
+            lib.fpsgpu_debug_fail_allocations(-1)
+        tickets = [srv.submit(p, k, h, s) for p, k, h, s in reqs]
+        for t, w in zip(tickets, want):
+            np.testing.assert_array_equal(srv.result(t)[0], w)
