@@ -127,7 +127,42 @@ int allow_cluster16(const void* func) {
     return FPSGPU_OK;
 }
 void set_thread_pool(cudaMemPool_t pool) { t_pool = pool; }
-cudaMemPool_t thread_pool() { return t_pool; }
+
+namespace {
+// Scratch memory the library keeps mapped between calls on each device.  The
+// device's default pool returns freed memory to the driver at every
+// synchronisation (release threshold 0), so each call would map its scratch
+// again: about 2 GB for a 16.7M-point cloud, several ms per call.
+constexpr uint64_t kKeepMappedBytes = 8ull << 30;
+std::mutex g_pool_mu;
+std::vector<cudaMemPool_t> g_pools;  // per device; null until first use
+}  // namespace
+
+cudaMemPool_t thread_pool() {
+    if (t_pool) return t_pool;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if ((int)g_pools.size() <= dev) g_pools.resize(dev + 1, nullptr);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return nullptr;  // fall back to the device's default pool
+        }
+        uint64_t keep = kKeepMappedBytes;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        g_pools[dev] = pool;
+    }
+    return g_pools[dev];
+}
 
 // Cluster size of the batched engine's cluster sampler: FPSGPU_CLUSTER_SIZE
 // (1 turns clusters off; 2, 4, 8 or 16), default 8; clouds that need more CTAs

@@ -37,9 +37,11 @@ int current_ctx(DevCtx* ctx);
 
 // Stream-ordered scratch: every allocation is released with cudaFreeAsync on
 // the same stream when the object goes out of scope.
-// The memory pool that stream-ordered scratch of the calling thread comes from
-// (null: the device's default pool).  Server workers each use their own pool:
-// the default pool may make one stream wait for another stream's work in order
+// The memory pool that stream-ordered scratch of the calling thread comes from:
+// the one set for the thread, else the library's pool of the current device
+// (it keeps up to 8 GB mapped between calls), else, if that pool cannot be
+// made, the device's default pool.  Server workers each use their own pool:
+// a shared pool may make one stream wait for another stream's work in order
 // to reuse memory freed there, which would chain independent batches together.
 void set_thread_pool(cudaMemPool_t pool);
 cudaMemPool_t thread_pool();
