@@ -107,3 +107,22 @@ def test_random_start_uses_numpy_global_state():
     assert a == np.random.randint(low=0, high=1000)
     assert isinstance(fps.get_start_idx(10, [1, 2]), np.ndarray)
     assert fps.get_start_idx(10, [1, 2]).dtype == np.uint64
+
+
+def test_import_raises_the_hardware_work_queues_unless_set():
+    """Importing the package sets CUDA_DEVICE_MAX_CONNECTIONS=32 (the request
+    server's worker streams must not share hardware queues) but keeps a value
+    the caller chose."""
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = "import os, fpsample_gb300; print(os.environ['CUDA_DEVICE_MAX_CONNECTIONS'])"
+    for preset, want in ((None, "32"), ("16", "16")):
+        env = {k: v for k, v in os.environ.items() if k != "CUDA_DEVICE_MAX_CONNECTIONS"}
+        if preset is not None:
+            env["CUDA_DEVICE_MAX_CONNECTIONS"] = preset
+        out = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
+                             text=True, check=True).stdout.strip()
+        assert out == want
