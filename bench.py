@@ -543,7 +543,7 @@ def run_gpu_arm(args):
 
 
 def run_served(args):
-    """configs[3]: a Poisson stream of requests (2000/s) into the request server.
+    """The served workload: a Poisson stream of requests (2000/s) into the request server.
     The first --served-window seconds of the 10 s stream are replayed at their
     arrival times (the full stream would need ~80 GB of host memory for its
     points).  Reports completed requests/s over the replay, the latency
@@ -645,8 +645,8 @@ def run_latency_probe(args):
 
 def run_peaks_probe(args):
     """Shared-memory and L2 read bandwidth of this GPU (the roofline of vanilla
-    FPS on clouds that stay on chip), best of five, beside the driver-measured
-    HBM figure."""
+    FPS on clouds that stay on chip), best of five, beside the HBM copy
+    bandwidth measured for this GPU type (MEASURED_PEAKS.json)."""
     import torch
 
     from fpsample_gb300 import capi

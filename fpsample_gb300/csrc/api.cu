@@ -130,7 +130,7 @@ void set_thread_pool(cudaMemPool_t pool) { t_pool = pool; }
 
 namespace {
 // Scratch memory the library keeps mapped between calls on each device.  The
-// device's default pool returns freed memory to the driver at every
+// device's default pool releases freed memory back to the system at every
 // synchronisation (release threshold 0), so each call would map its scratch
 // again: about 2 GB for a 16.7M-point cloud, several ms per call.
 constexpr uint64_t kKeepMappedBytes = 8ull << 30;

@@ -1,7 +1,7 @@
 // Bandwidth microbenchmarks for the roofline of the on-chip levels: aggregate
 // shared-memory read bandwidth and L2 read bandwidth of this GPU.  The vanilla
 // FPS configurations whose cloud stays on chip are bounded by these, not by
-// HBM; the measured HBM copy bandwidth covers the rest.  Diagnostics
+// HBM; the measured HBM copy bandwidth of this GPU type covers the rest.  Diagnostics
 // only: nothing on the sampling path calls them.
 #include <cuda_runtime.h>
 

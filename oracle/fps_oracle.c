@@ -3,7 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the oracle: it is loaded by the
  * tests, by __graft_entry__.smoke() and by bench.py's CPU-baseline /
- * reference arm, and only as the checker (or the timed CPU baseline).  The
+ * reference arm, and only as the answer GPU results are compared with (or the
+ * timed CPU baseline).  The
  * product (libfpsgpu + fpsample_gb300) never links, loads or calls it and
  * has no CPU fallback.
  *

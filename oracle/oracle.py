@@ -1,8 +1,9 @@
 """Python handle on the oracle.
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline / reference arm, always as the checker or the timed
-CPU baseline.  The product package (fpsample_gb300) never imports it.
+bench.py's CPU-baseline / reference arm, always as the reference answer that
+GPU results are compared with, or as the timed CPU baseline.  The product
+package (fpsample_gb300) never imports it.
 
 Two things live here:
 
