@@ -126,3 +126,40 @@ def test_import_raises_the_hardware_work_queues_unless_set():
         out = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
                              text=True, check=True).stdout.strip()
         assert out == want
+
+
+@pytest.mark.parametrize(
+    "call",
+    [
+        lambda: fps.bucket_fps_kdline_sampling_batch([PC, PC[:, :2]], 4, 3),   # mixed dimensions
+        lambda: fps.bucket_fps_kdline_sampling_batch([PC, PC], [4, 65], 3),    # K > n
+        lambda: fps.bucket_fps_kdline_sampling_batch([PC, PC], 4, [3, 7]),     # 2**h > n
+        lambda: fps.bucket_fps_kdline_sampling_batch([PC, PC], 4, 3, [0, 64]),  # start out of range
+        lambda: fps.bucket_fps_kdline_sampling_batch([PC, PC], [4], 3),        # one K per cloud
+        lambda: fps.bucket_fps_kdline_sampling_batch([PC, PC], 4, [0, 3]),     # h >= 1
+    ],
+)
+def test_batch_wrapper_checks(call):
+    with pytest.raises(AssertionError):
+        call()
+
+
+def test_batch_list_extension_checks_and_no_cpu_fallback():
+    a = np.zeros((10, 3), np.float32)
+    u = lambda *v: np.array(v, np.uint64)
+    assert fps.bucket_fps_kdline_sampling_batch([], 4, 3) == []
+    with pytest.raises(ValueError, match="one entry per cloud"):
+        _fpsample._bucket_fps_kdline_sampling_batch_list([a, a], u(2), u(1, 1), u(0, 0))
+    with pytest.raises(ValueError, match="empty cloud"):
+        _fpsample._bucket_fps_kdline_sampling_batch_list([a, a[:0]], u(2, 1), u(1, 1), u(0, 0))
+    with pytest.raises(ValueError, match="same dimension"):
+        _fpsample._bucket_fps_kdline_sampling_batch_list([a, a[:, :2]], u(2, 2), u(1, 1), u(0, 0))
+    with pytest.raises(ValueError, match="start_idx"):
+        _fpsample._bucket_fps_kdline_sampling_batch_list([a], u(2), u(1), u(10))
+    # a valid batch: sampled on the GPU, or a loud failure where there is none
+    try:
+        out = _fpsample._bucket_fps_kdline_sampling_batch_list([a], u(2), u(1), u(0))
+    except RuntimeError as e:
+        assert "fpsgpu_kdline_batch_list failed with error code 4" in str(e)
+    else:
+        assert out.shape == (2,)
