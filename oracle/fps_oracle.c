@@ -277,11 +277,13 @@ static int push_delay(bucket_t *bk, size_t pos) {
  * (FLT_MAX-capped; trace[0] = FLT_MAX).
  * perm_out (optional, n): the build permutation.
  */
-int oracle_kdline(const float *pts, size_t n, size_t dim, size_t k, size_t start_idx,
-                  size_t height, int fma_mode, uint64_t *out, float *trace,
-                  uint64_t *perm_out) {
-    if (dim == 0 || dim > 8) return ORACLE_BAD_DIM;
-    if (start_idx >= n) return ORACLE_BAD_START;
+/* The body below is instantiated per (dim, fma_mode) by oracle_kdline, so the
+   distance loops unroll as they do in the reference, whose buckets are
+   templated on the dimension (wrapper.hpp:45-60 dispatches DIM 1..8); the
+   arithmetic is the same in every instance. */
+static inline __attribute__((always_inline)) int kdline_sample(
+    const float *pts, size_t n, const size_t dim, size_t k, size_t start_idx, size_t height,
+    const int fma_mode, uint64_t *out, float *trace, uint64_t *perm_out) {
     int rc = ORACLE_OK;
     uint64_t *perm = (uint64_t *)malloc(n * sizeof(uint64_t));
     uint64_t *bstart = (uint64_t *)malloc(n * sizeof(uint64_t));
@@ -390,6 +392,29 @@ free_buckets:
 done:
     free(perm); free(bstart); free(w); free(dis);
     return rc;
+}
+
+int oracle_kdline(const float *pts, size_t n, size_t dim, size_t k, size_t start_idx,
+                  size_t height, int fma_mode, uint64_t *out, float *trace,
+                  uint64_t *perm_out) {
+    if (dim == 0 || dim > 8) return ORACLE_BAD_DIM;
+    if (start_idx >= n) return ORACLE_BAD_START;
+#define ORACLE_KDLINE_CASE(D)                                                                  \
+    case D:                                                                                    \
+        return fma_mode ? kdline_sample(pts, n, D, k, start_idx, height, 1, out, trace, perm_out) \
+                        : kdline_sample(pts, n, D, k, start_idx, height, 0, out, trace, perm_out);
+    switch (dim) {
+        ORACLE_KDLINE_CASE(1)
+        ORACLE_KDLINE_CASE(2)
+        ORACLE_KDLINE_CASE(3)
+        ORACLE_KDLINE_CASE(4)
+        ORACLE_KDLINE_CASE(5)
+        ORACLE_KDLINE_CASE(6)
+        ORACLE_KDLINE_CASE(7)
+        ORACLE_KDLINE_CASE(8)
+    }
+#undef ORACLE_KDLINE_CASE
+    return ORACLE_BAD_DIM;
 }
 
 /*
