@@ -60,6 +60,7 @@ class Scratch {
     Scratch& operator=(const Scratch&) = delete;
     template <class T>
     int alloc(T** out, size_t count) {
+        *out = nullptr;
         void* p = nullptr;
         size_t bytes = count ? count * sizeof(T) : sizeof(T);
         if (scratch_alloc_refused())
