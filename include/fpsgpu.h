@@ -9,6 +9,10 @@
  *   - return 0 on success, a positive FPSGPU_ERR_* code otherwise, with a
  *     message for the calling thread in fpsgpu_last_error();
  *   - every call runs on the CUDA device that is current on the calling thread;
+ *   - scratch memory is stream-ordered and comes from a memory pool the library
+ *     keeps per device, which holds up to 8 GB mapped between calls (the
+ *     device's default pool would unmap it at every synchronisation); it is
+ *     given back when the process exits;
  *   - there is no CPU fallback: without a usable GPU the calls fail with
  *     FPSGPU_ERR_CUDA.
  *
