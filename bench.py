@@ -321,6 +321,83 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def _served_worker_init(folder):
+    sys.path.insert(0, ROOT)
+    _W["folder"] = folder
+    _W["impl"], _W["obj"] = _cpu_impl()
+
+
+def _served_worker_run(job):
+    i, k, h, s = job
+    pts = np.load(os.path.join(_W["folder"], f"{i}.npy"))
+    t0 = time.perf_counter()
+    _cpu_run(_W["impl"], _W["obj"], "kdline", pts, k, h, s)
+    return i, time.perf_counter() - t0
+
+
+def run_served_reference(args):
+    """The served workload on the reference's CPU path: every request of the
+    same replayed window is sampled once on the host cores (one process per
+    core, the reference samples a cloud on one thread) and its time measured;
+    the requests are then served first come, first served by that many cores
+    at their arrival times, which gives requests/s and the latency
+    percentiles of the GPU line."""
+    rank, _, _ = dist_env()
+    if rank != 0:
+        return
+    import heapq
+    import multiprocessing as mp
+
+    from fpsample_gb300 import workloads as W
+
+    reqs = [(r.arrival_s, r.points, r.k, h_for(r.points.shape[0]), r.start)
+            for r in W.request_stream(rate=2000.0, duration_s=args.served_window,
+                                      seed=W.SEEDS["served"])]
+    impl, _ = _cpu_impl()
+    cores = min(os.cpu_count() or 1, len(reqs))
+    with tempfile.TemporaryDirectory() as folder:
+        for i, (_, p, _, _, _) in enumerate(reqs):
+            np.save(os.path.join(folder, f"{i}.npy"), p)
+        jobs = sorted(((i, k, h, s) for i, (_, p, k, h, s) in enumerate(reqs)),
+                      key=lambda j: -reqs[j[0]][1].shape[0] * j[1])
+        with mp.get_context("spawn").Pool(cores, initializer=_served_worker_init,
+                                          initargs=(folder,)) as pool:
+            service = dict(pool.imap_unordered(_served_worker_run, jobs))
+    free = [0.0] * cores  # first come, first served on `cores` servers
+    lat, queue = [], []
+    for i, (a, _, _, _, _) in enumerate(reqs):
+        t = heapq.heappop(free)
+        start = max(t, a)
+        done = start + service[i]
+        heapq.heappush(free, done)
+        lat.append((done - a) * 1e3)
+        queue.append((start - a) * 1e3)
+    lat, queue = np.array(lat), np.array(queue)
+    wall = max(free)
+    small = np.array([p.shape[0] <= 65536 for _, p, _, _, _ in reqs])
+    pct = lambda x, q: float(np.percentile(x, q)) if len(x) else None
+    v = len(reqs) / wall
+    line = {
+        "impl": "reference", "metric": "requests/sec (served)", "value": v, "unit": "requests/s",
+        "n_gpus": 0, "higher_is_better": True, "data": "synthetic (seeded generators)",
+        "config": {"workload": "served", "offered_rate_per_s": 2000, "window_s": args.served_window,
+                   "requests": len(reqs),
+                   "points_total": int(sum(p.shape[0] for _, p, _, _, _ in reqs)),
+                   "samples_total": int(sum(k for _, _, k, _, _ in reqs))},
+        "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max())},
+        "latency_ms_n_le_65536": {"p50": pct(lat[small], 50), "p99": pct(lat[small], 99),
+                                  "count": int(small.sum())},
+        "queue_ms": {"p50": pct(queue, 50), "p99": pct(queue, 99)},
+        "samples_per_s": sum(k for _, _, k, _, _ in reqs) / wall, "wall_s": wall,
+        "cpu_baseline": {"value": v, "unit": "requests/s", "cores": cores, "kind": impl,
+                         "sample": f"every request of the {args.served_window} s window timed once "
+                                   f"on {cores} processes, served first come first served by "
+                                   f"{cores} cores at the arrival times"},
+        "e2e": {"value": v, "unit": "requests/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def config_of(wl: Workload):
     name, clouds = wl.name, wl.clouds
     ns = [p.shape[0] for p, _, _, _ in clouds]
@@ -684,8 +761,8 @@ def main():
     if args.probe == "peaks":
         run_peaks_probe(args)
         return
-    if args.workload == "served" and args.impl != "reference":
-        run_served(args)
+    if args.workload == "served":
+        run_served(args) if args.impl != "reference" else run_served_reference(args)
         return
     if args.impl == "reference":
         run_reference_arm(args)

@@ -71,3 +71,18 @@ def test_reference_arm_prints_on_rank_zero_only():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["cores"] >= 1
+
+
+def test_served_reference_arm_line():
+    """bench.py --impl reference --workload served: the requests of the
+    replayed window timed on the host cores and served first come, first
+    served, reported in the GPU served line's units."""
+    env = dict(os.environ, PYTHONPATH=ROOT)
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--workload", "served", "--served-window", "0.0015"],
+                       capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"] == "requests/sec (served)"
+    assert line["config"]["requests"] == 1 and line["value"] > 0
+    assert line["latency_ms"]["p50"] > 0 and line["cpu_baseline"]["cores"] == 1
