@@ -77,3 +77,35 @@ def test_fp64_trace_close_to_fp32():
     idx, tr = ORACLE.fps(pts, 200, 0, "nofma", trace=True)
     ref = fp64_trace(pts, idx)
     np.testing.assert_allclose(tr[1:], ref[1:], rtol=1e-5)
+
+
+@pytest.mark.parametrize("mode", ["nofma", "fma"])
+def test_oracle_matches_the_live_reference_on_random_clouds(mode):
+    """Beyond the golden vectors: random clouds (continuous, integer grids full
+    of ties, Gaussian), every dimension 1..8, random heights, sample counts and
+    starts, against the reference compiled from its own sources -- where that
+    build exists (it does not on hosts without the reference's sources)."""
+    from oracle import oracle as O
+
+    if not O.reference_available(mode):
+        pytest.skip("the reference build is not available on this host")
+    ref = O.load_reference(mode)
+    rng = np.random.default_rng(2024 if mode == "nofma" else 4202)
+    for i in range(24):
+        d = 1 + i % 8
+        n = int(np.exp(rng.uniform(np.log(16), np.log(12000))))
+        kind = i % 3
+        if kind == 0:
+            p = rng.random((n, d)) * rng.uniform(0.1, 50, d)
+        elif kind == 1:
+            p = rng.integers(0, 7, (n, d)).astype(np.float64)
+        else:
+            p = rng.standard_normal((n, d)) * 20
+        p = p.astype(np.float32)
+        h = int(rng.integers(1, max(1, int(np.log2(n))) + 1))
+        k = int(rng.integers(1, min(n, 1500) + 1))
+        s = int(rng.integers(0, n))
+        np.testing.assert_array_equal(ORACLE.kdline(p, k, h, s, mode),
+                                      ref.bucket_fps_kdline_sampling(p, k, h, s))
+        np.testing.assert_array_equal(ORACLE.fps(p, min(k, 300), s, mode),
+                                      ref.fps_sampling(p, min(k, 300), s))
