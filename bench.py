@@ -86,7 +86,7 @@ class Workload:
 
 
 def workload(name: str) -> Workload:
-    from fpsample_gb300 import workloads as W
+    import workloads as W
 
     if name == "batched-256":
         clouds = W.batched_clouds(seed=W.SEEDS["batched-256"])
@@ -197,26 +197,47 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU side: oracle / reference
 # ---------------------------------------------------------------------------
+def fp_mode() -> str:
+    """The distance arithmetic both arms run: FPSAMPLE_FP_MODE, else the mode
+    of the reference's stock build on this host ("fma" on aarch64, where GCC
+    contracts a*b+c by default; "nofma" on x86-64).  The GPU library picks the
+    same default by itself; the reference arm must not import it."""
+    import platform
+
+    m = os.environ.get("FPSAMPLE_FP_MODE", "").lower()
+    if m in ("fma", "nofma"):
+        return m
+    return "fma" if platform.machine() in ("aarch64", "arm64") else "nofma"
+
+
 def _cpu_impl():
     """('reference', module) when the reference compiled from its own sources
-    is importable here, else ('port', Oracle)."""
+    (oracle/_ref, built for this host by `make -C oracle ref`) is importable
+    here, else ('port', Oracle): the C restatement."""
     from oracle import oracle as O
 
-    mode = os.environ.get("FPSAMPLE_FP_MODE", "nofma")
-    if O.reference_available(mode):
-        return "reference", O.load_reference(mode)
+    if O.reference_available(fp_mode()):
+        return "reference", O.load_reference(fp_mode())
     return "port", O.Oracle()
 
 
 def _cpu_run(impl, obj, algo, pts, k, h, start):
-    mode = os.environ.get("FPSAMPLE_FP_MODE", "nofma")
     if algo == "vanilla":
         if impl == "reference":
             return obj.fps_sampling(pts, k, start)
-        return obj.fps(pts, k, start, mode)
+        return obj.fps(pts, k, start, fp_mode())
     if impl == "reference":
         return obj.bucket_fps_kdline_sampling(pts, k, h, start)
-    return obj.kdline(pts, k, h, start, mode)
+    return obj.kdline(pts, k, h, start, fp_mode())
+
+
+def _cpu_describe(impl: str) -> str:
+    from oracle import oracle as O
+
+    if impl == "reference":
+        return (f"the reference's own src/lib.cpp compiled on this host ({fp_mode()} build: "
+                f"{O.reference_build_flags(fp_mode())})")
+    return f"the oracle port oracle/fps_oracle.c ({fp_mode()} arithmetic)"
 
 
 def _cpu_cloud_seconds(impl, obj, algo, p, k, h, s):
@@ -266,7 +287,7 @@ def cpu_baseline(wl: Workload, budget_s: float = 12.0):
         if time.perf_counter() - t0 > budget_s:
             break
     sample = (f"first {done} of {len(wl.clouds)} clouds ({pts_done} points), one thread, "
-              f"{secs:.1f} s of {wl.algo}")
+              f"{secs:.1f} s of {wl.algo} on {_cpu_describe(impl)}")
     if how:
         sample += f"; {how}"
     return {"value": done / secs, "unit": UNIT, "cores": 1, "kind": impl, "sample": sample}
@@ -316,7 +337,8 @@ def run_reference_arm(args):
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": impl,
                              "sample": f"{copies} cop{'y' if copies == 1 else 'ies'} of all "
                                        f"{len(clouds)} clouds per step, {cores} processes, "
-                                       f"{wl.algo}" + (f"; per cloud: {how}" if how else "")},
+                                       f"{wl.algo} on {_cpu_describe(impl)}"
+                                       + (f"; per cloud: {how}" if how else "")},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -348,7 +370,7 @@ def run_served_reference(args):
     import heapq
     import multiprocessing as mp
 
-    from fpsample_gb300 import workloads as W
+    import workloads as W
 
     reqs = [(r.arrival_s, r.points, r.k, h_for(r.points.shape[0]), r.start)
             for r in W.request_stream(rate=2000.0, duration_s=args.served_window,
@@ -408,17 +430,122 @@ def config_of(wl: Workload):
             "h": ("size class: 5 (<8K), 7 (<256K), 9" if name == "batched-256"
                   else (clouds[0][2] if wl.algo == "kdline" else None)),
             "start_idx": 0, "l2": "flushed before every step (256 MiB write)",
-            "parallelism": "replicas"}
+            "fp_mode": fp_mode(), "parallelism": "replicas"}
 
 
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def _peaks():
+    """(HBM GB/s and where it comes from, on-chip peaks {smem_gbs, l2_gbs})."""
+    try:
+        hbm = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+        src = "MEASURED_PEAKS.json hbm_gbs (of measured)"
+    except (OSError, KeyError, ValueError):
+        hbm, src = 6800.0, "fallback 6800 GB/s (of fallback)"
+    try:
+        onchip = json.load(open(os.path.join(ROOT, "profiles", "peaks.json")))
+    except (OSError, ValueError):
+        onchip = {}
+    return hbm, src, onchip
+
+
+def roofline(wl: Workload, st: dict, steps: int, step_ms: float):
+    """The sampling kernel's roofline line and the vanilla-equivalent bytes.
+
+    Algorithmic bytes per launch (one launch samples every cloud of a step):
+      kd-line  sum over clouds of 2^h (8D + 8) (K - 1) B of bucket records
+               (box and max key of every bucket, once per sample) plus the
+               running distances recomputed x (4D + 8) B (coordinates, old and
+               new distance), the recomputed count taken from the device
+               counter, not assumed;
+      vanilla  N (K - 1) (4D + 8) B per cloud: every point read and its
+               running distance read and written once per sample.
+    achieved = those bytes / the kernel's average event-timed launch time,
+    against the measured HBM copy bandwidth; frac_l2 / frac_smem put the same
+    figure against the measured on-chip read bandwidths.  The pruned sampler
+    does not move all of these bytes: actual_* counts what it touches (boxes
+    tested x (8D + 8) + distances recomputed x (4D + 8))."""
+    d = wl.dim
+    launches = max(1, st["sampler_launches"])
+    launch_ms = st["sampler_ms"] / launches
+    per_step = launches / max(1, steps)  # sampler launches per step
+    touched = st["points_touched"] / launches
+    tested = st["pieces_tested"] / launches
+    if wl.algo == "kdline":
+        alg = sum((2 ** h) * (8 * d + 8) * (k - 1) for _, k, h, _ in wl.clouds) / per_step \
+            + touched * (4 * d + 8)
+        rule = "sum 2^h (8D+8)(K-1) + recomputed distances x (4D+8)"
+    else:
+        alg = sum(p.shape[0] * (k - 1) * (4 * d + 8) for p, k, _, _ in wl.clouds) / per_step
+        rule = "N (K-1) (4D+8)"
+    actual = tested * (8 * d + 8) + touched * (4 * d + 8)
+    hbm, src, onchip = _peaks()
+    sec = launch_ms / 1e3
+    achieved = alg / sec / 1e9 if sec > 0 else None
+    act_gbs = actual / sec / 1e9 if sec > 0 else None
+    samples = sum(k for _, k, _, _ in wl.clouds) / per_step
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm if achieved else None, "kernel": "sampler",
+            "alg_bytes_per_launch": alg, "alg_bytes_rule": rule, "launch_ms": launch_ms,
+            "peak_source": src,
+            "frac_l2": achieved / onchip["l2_gbs"] if achieved and onchip.get("l2_gbs") else None,
+            "frac_smem": (achieved / onchip["smem_gbs"]
+                          if achieved and onchip.get("smem_gbs") else None),
+            "onchip_peaks_source": "profiles/peaks.json (bench.py --probe peaks)" if onchip else None,
+            "actual_bytes_per_launch": actual, "actual_gbs": act_gbs,
+            "actual_frac": act_gbs / hbm if act_gbs else None,
+            "boxes_tested_per_sample": tested / samples if samples else None,
+            "distances_recomputed_per_sample": touched / samples if samples else None}
+    veq = None
+    if wl.algo == "vanilla":
+        b = sum(p.shape[0] * (k - 1) * (4 * d + 8) for p, k, _, _ in wl.clouds)
+        veq = {"bytes_per_step": b, "gbs_whole_step": b / (step_ms / 1e3) / 1e9}
+    return roof, veq
+
+
+def _check_worker(job):
+    from oracle.oracle import Oracle
+
+    i, algo, p, k, h, s, mode = job
+    orc = _W.get("orc") or _W.setdefault("orc", Oracle())
+    want = orc.fps(p, k, s, mode) if algo == "vanilla" else orc.kdline(p, k, h, s, mode)
+    return i, want
+
+
+def check_step(wl: Workload, res, koffs, mode: str):
+    """(all equal, what was checked): the GPU's complete output for the step
+    against the reference answers -- the committed full-size fixtures
+    (tests/golden/fullsize.npz) for the one-cloud benchmark sizes, else the
+    oracle on every cloud (a process pool, outside the timed region)."""
+    from tests.golden import fullsize as F
+
+    case = F.BY_WORKLOAD.get(wl.name)
+    if case and F.available():
+        c = F.case(case)
+        if not F.input_matches(c["cloud"], wl.clouds[0][0]):
+            return False, f"input differs from the fixture's {c['cloud']} cloud (sha256)"
+        want = F.expected(case, mode)
+        ok = bool(np.array_equal(res[: len(want)], want)) and len(res) == len(want)
+        return ok, (f"all {len(want)} samples against tests/golden/fullsize.npz "
+                    f"{case}__{mode} (source: {c['source']})")
+    import multiprocessing as mp
+
+    jobs = [(i, wl.algo, p, k, h, s, mode) for i, (p, k, h, s) in enumerate(wl.clouds)]
+    jobs.sort(key=lambda j: -j[2].shape[0] * j[3])
+    ok = True
+    procs = max(1, min(len(jobs), os.cpu_count() or 1))
+    with mp.get_context("spawn").Pool(procs) as pool:
+        for i, want in pool.imap_unordered(_check_worker, jobs):
+            ok &= bool(np.array_equal(res[koffs[i]:koffs[i + 1]], want))
+    return ok, f"all {len(jobs)} clouds, every sample, against the oracle ({mode})"
+
+
 def run_gpu_arm(args):
     import torch
     import torch.distributed as dist
 
-    import fpsample_gb300 as fps
+    import fpsample as fps
     from fpsample_gb300 import capi
 
     rank, world, local = dist_env()
@@ -480,28 +607,12 @@ def run_gpu_arm(args):
         if world > 1:
             dist.barrier()
 
-    # correctness of what is timed: a few clouds against the oracle (outside timing)
-    from oracle.oracle import Oracle
-
-    orc = Oracle()
+    # correctness of what is timed, outside the timed region: every cloud of
+    # the step, every sample, against its reference answer
     step_device()
     torch.cuda.synchronize()
     res = d_out.cpu().numpy().astype(np.uint64)
-    check_ids = sorted(set(i for i in (0, 1, len(clouds) // 2, int(np.argmax(sizes)))
-                           if i < len(clouds)))
-    bit_exact = True
-    checked_prefix = {}
-    for i in check_ids:
-        p, k, h, s = clouds[i]
-        kt = truncated_k(wl.algo, p.shape[0], k)
-        kc = k if kt is None else kt  # FPS is prefix-stable in K
-        if wl.algo == "vanilla":
-            want = orc.fps(p, kc, s, fps.get_fp_mode())
-        else:
-            want = orc.kdline(p, kc, h, s, fps.get_fp_mode())
-        bit_exact &= bool(np.array_equal(res[koffs[i]:koffs[i] + kc], want))
-        if kt is not None:
-            checked_prefix[i] = kc
+    bit_exact, checked = check_step(wl, res, koffs, fps.get_fp_mode())
 
     for _ in range(args.warmup):
         flush.zero_()
@@ -553,33 +664,7 @@ def run_gpu_arm(args):
 
     if rank == 0:
         launches = int(st["kernel_launches"])
-        d = D
-        alg_bytes = st["pieces_tested"] * (8 * d + 8) + st["points_touched"] * (4 * d + 8)
-        per_launch_bytes = alg_bytes / max(1, st["sampler_launches"])
-        per_launch_ms = st["sampler_ms"] / max(1, st["sampler_launches"])
-        achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else None
-        peaks = {}
-        try:
-            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        except OSError:
-            pass
-        peak = peaks.get("hbm_gbs", 6800.0)
-        bound, peak_source = "hbm", "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"
-        vanilla_equiv = None
-        if wl.algo == "vanilla":
-            # vanilla-equivalent bytes: every running distance read and written
-            # and every point read once per sample, N (K-1) (4D + 8) B per cloud
-            veq = sum(p.shape[0] * (k - 1) * (4 * d + 8) for p, k, _, _ in clouds)
-            vanilla_equiv = {"bytes_per_step": veq, "gbs": veq / (ms / 1e3) / 1e9}
-            # a cloud that stays on chip is bounded by L2, not HBM
-            onchip = {}
-            try:
-                onchip = json.load(open(os.path.join(ROOT, "profiles", "peaks.json")))
-            except OSError:
-                pass
-            if host_all.nbytes * 2 <= 96 << 20 and onchip.get("l2_gbs"):
-                bound, peak = "l2", onchip["l2_gbs"]
-                peak_source = "profiles/peaks.json l2_gbs (bench.py --probe peaks)"
+        roof, vanilla_equiv = roofline(wl, st, args.steps, ms)
         traffic = None
         tpath = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tpath):
@@ -592,10 +677,9 @@ def run_gpu_arm(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded generators, fpsample_gb300.workloads)",
+            "data": "synthetic (seeded generators, workloads.py)",
             "config": config_of(wl),
-            "bit_exact_checked_clouds": check_ids, "bit_exact": bit_exact,
-            "bit_exact_prefix_checked": checked_prefix or None,
+            "bit_exact": bit_exact, "bit_exact_checked": checked,
             "vanilla_equivalent": vanilla_equiv,
             "plain_per_cloud": {"value": len(clouds) / (plain_ms / 1e3), "unit": UNIT,
                                 "ms_per_step": plain_ms, "identical_to_batched": plain_ok,
@@ -603,10 +687,7 @@ def run_gpu_arm(args):
             "e2e": {"value": e2e_v, "unit": UNIT,
                     "h2d_bytes_per_step": int(host_all.nbytes),
                     "d2h_bytes_per_step": int(koffs[-1]) * 8},
-            "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                         "kernel": "sampler", "alg_bytes_per_launch": per_launch_bytes,
-                         "launch_ms": per_launch_ms, "peak_source": peak_source},
+            "roofline": dict(roof, traffic=traffic),
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": launches,
@@ -629,7 +710,7 @@ def run_served(args):
     import threading
 
     from fpsample_gb300 import capi
-    from fpsample_gb300 import workloads as W
+    import workloads as W
 
     reqs = list(W.request_stream(rate=2000.0, duration_s=args.served_window,
                                  seed=W.SEEDS["served"]))
@@ -681,7 +762,7 @@ def run_latency_probe(args):
     import torch
 
     from fpsample_gb300 import capi
-    from fpsample_gb300 import workloads as W
+    import workloads as W
 
     def best_of(fn, reps=3):
         fn()

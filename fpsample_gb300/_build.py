@@ -1,8 +1,11 @@
 """In-tree build of the native parts of fpsample_gb300.
 
-Outputs (git-ignored, next to this file):
-  libfpsgpu.so          CUDA kernels + the C ABI of include/fpsgpu.h, sm_103a only
-  _fpsample<ext>        pybind11 extension (C++) calling the C ABI
+Outputs (git-ignored):
+  fpsample_gb300/libfpsgpu.so   CUDA kernels + the C ABI of include/fpsgpu.h,
+                                sm_103a only
+  fpsample/_fpsample<ext>       pybind11 extension (C++) calling the C ABI,
+                                importable as fpsample._fpsample like the
+                                reference's
 
 Each .cu translation unit is compiled by its own nvcc process in parallel;
 nothing is rebuilt when its output is newer than every source it depends on.
@@ -22,7 +25,7 @@ ROOT = os.path.dirname(HERE)
 INCLUDE = os.path.join(ROOT, "include")
 OBJ = os.path.join(HERE, "_objs")
 LIB = os.path.join(HERE, "libfpsgpu.so")
-EXT = os.path.join(HERE, "_fpsample" + sysconfig.get_config_var("EXT_SUFFIX"))
+EXT = os.path.join(ROOT, "fpsample", "_fpsample" + sysconfig.get_config_var("EXT_SUFFIX"))
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CU_UNITS = ["api", "vanilla_nofma", "vanilla_fma", "engine_nofma", "engine_fma", "noalloc", "server",
@@ -94,7 +97,7 @@ def build(verbose: bool = False) -> None:
         pyinc = sysconfig.get_paths()["include"]
         _run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-fvisibility=hidden",
               "-I" + pyinc, "-I" + _pybind11_include(), "-I" + INCLUDE, src,
-              "-o", EXT, "-L" + HERE, "-lfpsgpu", "-Wl,-rpath,$ORIGIN"])
+              "-o", EXT, "-L" + HERE, "-lfpsgpu", "-Wl,-rpath,$ORIGIN/../fpsample_gb300"])
 
 
 if __name__ == "__main__":

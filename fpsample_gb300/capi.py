@@ -98,7 +98,7 @@ def lib() -> ctypes.CDLL:
     global _lib
     if _lib is None:
         if not os.path.exists(LIB_PATH):
-            raise ImportError(f"{LIB_PATH} is not built (python -m fpsample_gb300._build)")
+            raise ImportError(f"{LIB_PATH} is not built (python fpsample_gb300/_build.py)")
         L = ctypes.CDLL(LIB_PATH)
         for name, (res, args) in SIGNATURES.items():
             f = getattr(L, name)

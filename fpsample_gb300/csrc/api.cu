@@ -435,13 +435,23 @@ __global__ void build_seed_refine(BuildArgs a) {
 // ---------------------------------------------------------------------------
 namespace {
 std::once_flag g_mode_once;
+// The default matches the reference as its own build recipe compiles it on
+// this host's architecture: GCC fuses a*b+c by default and aarch64 has a fused
+// multiply-add, so an aarch64 build contracts; the x86-64 baseline has no FMA
+// instruction, so an x86-64 build cannot.
+#if defined(__aarch64__)
+int g_fp_mode = FPSGPU_FP_FMA;
+#else
 int g_fp_mode = FPSGPU_FP_NOFMA;
+#endif
 std::mutex g_mode_mu;
 
 int fp_mode() {
     std::call_once(g_mode_once, [] {
         const char* e = std::getenv("FPSAMPLE_FP_MODE");
         if (e && (std::strcmp(e, "fma") == 0 || std::strcmp(e, "FMA") == 0)) g_fp_mode = FPSGPU_FP_FMA;
+        if (e && (std::strcmp(e, "nofma") == 0 || std::strcmp(e, "NOFMA") == 0))
+            g_fp_mode = FPSGPU_FP_NOFMA;
     });
     std::lock_guard<std::mutex> lk(g_mode_mu);
     return g_fp_mode;

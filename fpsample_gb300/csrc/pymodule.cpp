@@ -1,4 +1,4 @@
-// fpsample_gb300._fpsample: the Python extension module of the GPU build.
+// fpsample._fpsample: the Python extension module of the GPU build.
 //
 // It mirrors the reference's pybind11 module `fpsample._fpsample`
 // (src/lib.cpp:581-660): same function names, argument order, argument
@@ -319,7 +319,7 @@ PYBIND11_MODULE(_fpsample, m) {
         Farthest point sampling (FPS) on NVIDIA GB300
         -----------------------
 
-        .. currentmodule:: fpsample_gb300
+        .. currentmodule:: fpsample
 
         .. autosummary::
            :toctree: _generate

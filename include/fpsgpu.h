@@ -18,10 +18,12 @@
  *
  * Floating point: distances are computed exactly as the reference computes
  * them (fp32, dimensions summed in order).  Whether a*b+c is fused into an FMA
- * changes results, so the library has two modes (fpsgpu_set_fp_mode): the
- * default FPSGPU_FP_NOFMA matches a reference build that does not contract
- * (the default x86-64 build); FPSGPU_FP_FMA matches a contracting build (GCC's
- * default on aarch64, or x86-64 with -mfma).
+ * changes results, so the library has two modes (fpsgpu_set_fp_mode):
+ * FPSGPU_FP_NOFMA matches a reference build that does not contract (the
+ * default x86-64 build); FPSGPU_FP_FMA matches a contracting build (GCC's
+ * default on aarch64, or x86-64 with -mfma).  The default is the mode of the
+ * reference's stock build on the CPU architecture the library runs on: FMA on
+ * aarch64 hosts (Grace), NOFMA elsewhere.
  */
 #ifndef FPSGPU_H
 #define FPSGPU_H
@@ -204,7 +206,8 @@ int fpsgpu_kdline_build(const float *raw_data, size_t n_points, size_t dim,
 
 /* floating-point mode for subsequent calls from any thread (FPSGPU_FP_*).
    Initial value: environment variable FPSAMPLE_FP_MODE ("fma" / "nofma"),
-   else FPSGPU_FP_NOFMA. */
+   else the host architecture's stock reference build (FPSGPU_FP_FMA on
+   aarch64, FPSGPU_FP_NOFMA elsewhere). */
 int fpsgpu_set_fp_mode(int mode);
 int fpsgpu_get_fp_mode(void);
 

@@ -35,8 +35,10 @@
  * The file must be compiled with -ffp-contract=off so that mode 0 stays
  * uncontracted on compilers whose default contracts (GCC on aarch64).
  */
+#define _POSIX_C_SOURCE 200809L /* pthread barriers under -std=c11 */
 #include <float.h>
 #include <math.h>
+#include <pthread.h>
 #include <stddef.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -513,5 +515,196 @@ int oracle_kdtree(const float *pts, size_t n, size_t dim, size_t k, size_t start
     }
 done:
     free(perm); free(bstart); free(w); free(dis);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Vanilla FPS on several host threads                                       */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * The same answer as oracle_fps (src/lib.cpp:111-246), computed by n_threads
+ * threads so that clouds of tens of millions of points can be sampled to full
+ * K on the CPU.  Exactness rests on two facts:
+ *   - every running min-distance update (lib.cpp:214-221) reads only its own
+ *     point and the reference point, so the points can be split into
+ *     contiguous chunks, one per thread, with the same arithmetic per point;
+ *   - the reference's argmax scan with >= (lib.cpp:223-230) returns the LAST
+ *     index holding the largest value.  Each thread scans its chunk in index
+ *     order with >=, and the chunk results are folded in chunk order, again
+ *     with >=, which is that same sequential scan cut into pieces.
+ * Points are copied into one array per dimension so each thread streams them.
+ */
+
+typedef struct {
+    float v;
+    int valid;
+    size_t i;
+} mt_best_t;
+
+typedef struct {
+    const float *const *col; /* col[j][i]: coordinate j of point i */
+    float *dmin;
+    size_t n, dim, k, n_starts;
+    const uint64_t *starts;
+    int fma_mode;
+    size_t n_threads;
+    mt_best_t *slot;         /* [2][n_threads], double-buffered by step parity */
+    pthread_barrier_t *bar;
+    uint64_t *out;
+    float *trace;
+} mt_job_t;
+
+typedef struct {
+    mt_job_t *job;
+    size_t tid;
+} mt_arg_t;
+
+/* Running min-distance update of points [lo, hi) against ref, the
+   arithmetic of lib.cpp:214-221 per point (one column per dimension). */
+static inline __attribute__((always_inline)) void mt_update_body(
+    const float *const *col, float *dmin, size_t lo, size_t hi, size_t dim, const float *ref,
+    int fma_mode) {
+    if (fma_mode) {
+        for (size_t i = lo; i < hi; ++i) {
+            float acc = 0.0f;
+            for (size_t j = 0; j < dim; ++j) {
+                float d = col[j][i] - ref[j];
+                acc = fmaf(d, d, acc);
+            }
+            dmin[i] = acc < dmin[i] ? acc : dmin[i];
+        }
+    } else {
+        for (size_t i = lo; i < hi; ++i) {
+            float acc = 0.0f;
+            for (size_t j = 0; j < dim; ++j) {
+                float d = col[j][i] - ref[j];
+                float sq = d * d;
+                acc = acc + sq;
+            }
+            dmin[i] = acc < dmin[i] ? acc : dmin[i];
+        }
+    }
+}
+
+#if defined(__x86_64__) && defined(__GNUC__) && !defined(__clang__)
+/* The x86-64 baseline has no FMA instruction, so fmaf() is a library call per
+   point and dimension.  GCC also emits a clone for CPUs that have one, where
+   fmaf is a single instruction and the loop vectorises; fmaf's result is fully
+   specified by IEEE 754, so every clone computes the same values. */
+#define MT_CLONES __attribute__((target_clones("default", "fma")))
+#else
+#define MT_CLONES
+#endif
+
+MT_CLONES static void mt_update(const float *const *col, float *dmin, size_t lo, size_t hi,
+                                size_t dim, const float *ref, int fma_mode) {
+    switch (dim) {
+#define MT_CASE(D) \
+    case D: mt_update_body(col, dmin, lo, hi, D, ref, fma_mode); return;
+        MT_CASE(1) MT_CASE(2) MT_CASE(3) MT_CASE(4) MT_CASE(5) MT_CASE(6) MT_CASE(7) MT_CASE(8)
+#undef MT_CASE
+    default: mt_update_body(col, dmin, lo, hi, dim, ref, fma_mode);
+    }
+}
+
+static void *mt_worker(void *p) {
+    mt_arg_t *a = (mt_arg_t *)p;
+    mt_job_t *J = a->job;
+    const size_t T = J->n_threads, tid = a->tid;
+    const size_t lo = J->n * tid / T, hi = J->n * (tid + 1) / T;
+    float *dmin = J->dmin;
+    float ref[64];
+    size_t cur = (size_t)J->starts[0];
+    for (size_t t = 1; t < J->k; ++t) {
+        for (size_t j = 0; j < J->dim; ++j) ref[j] = J->col[j][cur];
+        mt_update(J->col, dmin, lo, hi, J->dim, ref, J->fma_mode);
+        mt_best_t b = {-1.0f, 0, 0};
+        for (size_t i = lo; i < hi; ++i) {
+            if (dmin[i] >= b.v) {
+                b.v = dmin[i];
+                b.i = i;
+                b.valid = 1;
+            }
+        }
+        mt_best_t *slots = J->slot + (t & 1) * T;
+        slots[tid] = b;
+        pthread_barrier_wait(J->bar);
+        /* every thread folds the chunk results in chunk order (the slots of
+           this parity are next written two steps later, after another barrier) */
+        mt_best_t g = {-1.0f, 0, 0};
+        for (size_t c = 0; c < T; ++c)
+            if (slots[c].valid && slots[c].v >= g.v) g = slots[c];
+        if (t < J->n_starts) {
+            cur = (size_t)J->starts[t];
+            if (tid == 0) {
+                J->out[t] = J->starts[t];
+                if (J->trace) J->trace[t] = INFINITY;
+            }
+        } else {
+            cur = g.i;  /* no valid chunk (all NaN): index 0, as the reference */
+            if (tid == 0) {
+                J->out[t] = g.i;
+                if (J->trace) J->trace[t] = g.v;
+            }
+        }
+    }
+    return NULL;
+}
+
+int oracle_fps_mt(const float *pts, size_t n, size_t dim, size_t k,
+                  const uint64_t *starts, size_t n_starts, int fma_mode,
+                  size_t n_threads, uint64_t *out, float *trace) {
+    if (n == 0 || dim == 0 || dim > 64) return ORACLE_BAD_ARG;
+    if (n_starts == 0 || n_starts > (k ? k : 1)) return ORACLE_BAD_ARG;
+    for (size_t s = 0; s < n_starts; ++s)
+        if (starts[s] >= n) return ORACLE_BAD_START;
+    if (k == 0) return ORACLE_OK;
+    if (n_threads == 0) n_threads = 1;
+    if (n_threads > n) n_threads = n;
+
+    int rc = ORACLE_OK;
+    float **col = (float **)calloc(dim, sizeof(float *));
+    float *dmin = (float *)malloc(n * sizeof(float));
+    mt_best_t *slot = (mt_best_t *)calloc(2 * n_threads, sizeof(mt_best_t));
+    pthread_t *th = (pthread_t *)calloc(n_threads, sizeof(pthread_t));
+    mt_arg_t *args = (mt_arg_t *)calloc(n_threads, sizeof(mt_arg_t));
+    pthread_barrier_t bar;
+    if (!col || !dmin || !slot || !th || !args) {
+        rc = ORACLE_NO_MEMORY;
+        goto done;
+    }
+    for (size_t j = 0; j < dim; ++j) {
+        col[j] = (float *)malloc(n * sizeof(float));
+        if (!col[j]) {
+            rc = ORACLE_NO_MEMORY;
+            goto done;
+        }
+        for (size_t i = 0; i < n; ++i) col[j][i] = pts[i * dim + j];
+    }
+    for (size_t i = 0; i < n; ++i) dmin[i] = INFINITY;
+    out[0] = starts[0];
+    if (trace) trace[0] = INFINITY;
+
+    mt_job_t job = {(const float *const *)col, dmin, n, dim, k, n_starts, starts, fma_mode,
+                    n_threads, slot, &bar, out, trace};
+    pthread_barrier_init(&bar, NULL, (unsigned)n_threads);
+    size_t started = 0;
+    for (; started < n_threads; ++started) {
+        args[started].job = &job;
+        args[started].tid = started;
+        if (pthread_create(&th[started], NULL, mt_worker, &args[started])) break;
+    }
+    if (started < n_threads) {
+        /* the barrier counts n_threads parties: the threads already running
+           would wait forever, so this cannot be recovered */
+        abort();
+    }
+    for (size_t t = 0; t < n_threads; ++t) pthread_join(th[t], NULL);
+    pthread_barrier_destroy(&bar);
+done:
+    if (col)
+        for (size_t j = 0; j < dim; ++j) free(col[j]);
+    free(col); free(dmin); free(slot); free(th); free(args);
     return rc;
 }

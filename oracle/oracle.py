@@ -12,8 +12,11 @@ Two things live here:
   file:line for every step).
 * ``load_reference(mode)``: the unmodified reference package, assembled from
   its own ``src/fpsample/__init__.py`` and the extension that ``make -C oracle
-  ref`` compiled from its own ``src/lib.cpp``.  Only available where the
-  reference sources are mounted; used to generate and check golden vectors.
+  ref`` compiled from its own ``src/lib.cpp``.  Both come from the copy of the
+  reference's sources that ``make -C oracle stage`` places in the git-ignored
+  ``baseline/_ref/``; where that copy is absent, so is the reference.  Used to
+  generate and check golden vectors and, on the host that runs the GPU, as the
+  timed reference CPU path.
 """
 from __future__ import annotations
 
@@ -28,7 +31,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
-REF_SRC = "/root/reference/src/fpsample"
+ROOT = os.path.dirname(HERE)
+REF_SRC = os.path.join(ROOT, "baseline", "_ref", "src", "fpsample")
+REF_FLAGS = os.path.join(HERE, "_ref", "flags.txt")
 
 FP_MODES = {"nofma": 0, "fma": 1}
 
@@ -59,11 +64,13 @@ class Oracle:
             build()
         lib = ctypes.CDLL(path)
         lib.oracle_fps.argtypes = [_f32p, _sz, _sz, _sz, _u64p, _sz, ctypes.c_int, _u64p, _f32p]
+        lib.oracle_fps_mt.argtypes = [_f32p, _sz, _sz, _sz, _u64p, _sz, ctypes.c_int, _sz, _u64p,
+                                      _f32p]
         lib.oracle_kdline.argtypes = [_f32p, _sz, _sz, _sz, _sz, _sz, ctypes.c_int, _u64p, _f32p, _u64p]
         lib.oracle_kdline_direct.argtypes = [_f32p, _sz, _sz, _sz, _sz, _sz, ctypes.c_int, _u64p]
         lib.oracle_kdtree.argtypes = [_f32p, _sz, _sz, _sz, _sz, ctypes.c_int, _u64p]
         lib.oracle_kdline_build.argtypes = [_f32p, _sz, _sz, _sz, _u64p, _u64p, ctypes.POINTER(_sz)]
-        for f in ("oracle_fps", "oracle_kdline", "oracle_kdline_direct", "oracle_kdline_build",
+        for f in ("oracle_fps", "oracle_fps_mt", "oracle_kdline", "oracle_kdline_direct", "oracle_kdline_build",
                   "oracle_kdtree"):
             getattr(lib, f).restype = ctypes.c_int
         self.lib = lib
@@ -85,6 +92,21 @@ class Oracle:
                                  _ptr(tr, _f32p) if trace else None)
         if rc:
             raise RuntimeError(f"oracle_fps failed with code {rc}")
+        return (out, tr) if trace else out
+
+    def fps_mt(self, pc, k, starts, fp_mode="nofma", threads=None, trace=False):
+        """Vanilla FPS on several host threads: the same answer as fps() (the
+        per-point updates are independent and the argmax folds exactly)."""
+        pc = self._pts(pc)
+        st = np.atleast_1d(np.asarray(starts, dtype=np.uint64))
+        out = np.zeros(k, np.uint64)
+        tr = np.zeros(k, np.float32) if trace else None
+        nt = threads or os.cpu_count() or 1
+        rc = self.lib.oracle_fps_mt(_ptr(pc, _f32p), pc.shape[0], pc.shape[1], k, _ptr(st, _u64p),
+                                    st.size, FP_MODES[fp_mode], nt, _ptr(out, _u64p),
+                                    _ptr(tr, _f32p) if trace else None)
+        if rc:
+            raise RuntimeError(f"oracle_fps_mt failed with code {rc}")
         return (out, tr) if trace else out
 
     def kdline(self, pc, k, h, start, fp_mode="nofma", trace=False, perm=False):
@@ -151,6 +173,30 @@ def fp64_trace(pc, idx):
         best[i:] = np.minimum(best[i:], d)
         out[i] = best[i]
     return out
+
+
+def stock_mode():
+    """The FP mode of this host's stock build of the reference (default flags:
+    "fma" where GCC contracts by default, i.e. aarch64; "nofma" on x86-64), or
+    None when the reference was not compiled here."""
+    try:
+        for line in open(REF_FLAGS):
+            if line.startswith("stock="):
+                return line.strip().split("=", 1)[1]
+    except OSError:
+        pass
+    return None
+
+
+def reference_build_flags(mode: str) -> str | None:
+    """The compiler flags `make ref` used for that build on this host."""
+    try:
+        for line in open(REF_FLAGS):
+            if line.startswith(mode + "="):
+                return line.strip().split("=", 1)[1]
+    except OSError:
+        pass
+    return None
 
 
 def reference_available(mode: str = "nofma") -> bool:

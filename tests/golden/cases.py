@@ -5,7 +5,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from fpsample_gb300 import workloads as W
+import workloads as W
 
 
 def _grid(n, d, levels, seed):

@@ -39,11 +39,37 @@ def test_library_exports_every_declared_symbol():
 
 def test_version_and_fp_mode_roundtrip():
     assert capi.lib().fpsgpu_version().decode().startswith("1.0.2")
-    capi.set_fp_mode("fma")
-    assert capi.get_fp_mode() == "fma"
-    capi.set_fp_mode("nofma")
-    assert capi.get_fp_mode() == "nofma"
-    assert capi.lib().fpsgpu_set_fp_mode(7) == 3
+    before = capi.get_fp_mode()
+    try:
+        capi.set_fp_mode("fma")
+        assert capi.get_fp_mode() == "fma"
+        capi.set_fp_mode("nofma")
+        assert capi.get_fp_mode() == "nofma"
+        assert capi.lib().fpsgpu_set_fp_mode(7) == 3
+    finally:
+        capi.set_fp_mode(before)
+
+
+def test_default_fp_mode_follows_the_host_architecture():
+    # the reference's stock build contracts a*b+c on aarch64 (GCC's default
+    # there) and cannot on x86-64; the library starts in the matching mode
+    # unless FPSAMPLE_FP_MODE says otherwise
+    import os
+    import platform
+    import subprocess
+    import sys
+
+    code = "from fpsample_gb300 import capi; print(capi.get_fp_mode())"
+    env = {k: v for k, v in os.environ.items() if k != "FPSAMPLE_FP_MODE"}
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                         cwd=os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    want = "fma" if platform.machine() in ("aarch64", "arm64") else "nofma"
+    assert out.stdout.strip() == want, out.stderr
+    for forced in ("fma", "nofma"):
+        out = subprocess.run([sys.executable, "-c", code], env=dict(env, FPSAMPLE_FP_MODE=forced),
+                             capture_output=True, text=True,
+                             cwd=os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+        assert out.stdout.strip() == forced, out.stderr
 
 
 def _kdline_rc(n, dim, start, k=4, h=3):

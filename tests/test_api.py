@@ -4,8 +4,8 @@ GPU every sampling call fails loudly instead of falling back to the CPU."""
 import numpy as np
 import pytest
 
-import fpsample_gb300 as fps
-from fpsample_gb300 import _fpsample
+import fpsample as fps
+from fpsample import _fpsample
 
 PC = np.random.default_rng(0).random((64, 3))
 

@@ -14,7 +14,7 @@
 import numpy as np
 import pytest
 
-import fpsample_gb300 as fps
+import fpsample as fps
 from fpsample_gb300 import capi
 from oracle.oracle import Oracle
 
@@ -74,7 +74,7 @@ def test_request_server_fails_requests_cleanly_and_keeps_serving():
     """A batch whose scratch allocation is refused fails its requests with
     FPSGPU_ERR_CUDA; the server's workers carry on and later requests are
     exact."""
-    from fpsample_gb300 import workloads as W
+    import workloads as W
 
     lib = capi.lib()
     rng = np.random.default_rng(73)

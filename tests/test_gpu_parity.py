@@ -2,19 +2,23 @@
 
 Sources of truth, in order:
   1. golden vectors produced by the unmodified reference (tests/golden/);
-  2. the oracle (oracle/fps_oracle.c, itself pinned to 1.) on seeded inputs;
-  3. at full workload sizes, where the oracle is too slow, oracle prefixes plus
-     size-independent FPS properties (non-increasing max-min trace, fp64 trace).
+  2. complete answers at the benchmark sizes (tests/golden/fullsize.npz: the
+     reference itself, or for the 16.7M-point vanilla case the multithreaded
+     oracle, see tests/golden/make_fullsize.py);
+  3. the oracle (oracle/fps_oracle.c, itself pinned to 1.) on seeded inputs;
+  plus size-independent FPS properties (non-increasing max-min trace, fp64
+  trace).
 Indices are compared exactly; the fp32 trace against an fp64 recomputation
 within rtol 1e-5.
 """
 import numpy as np
 import pytest
 
-import fpsample_gb300 as fps
+import fpsample as fps
 from fpsample_gb300 import capi
-from fpsample_gb300 import workloads as W
+import workloads as W
 from oracle.oracle import Oracle, fp64_trace
+from tests.golden import fullsize as F
 from tests.golden.golden import load_cases
 
 pytestmark = pytest.mark.gpu
@@ -26,9 +30,10 @@ MODES = ["nofma", "fma"]
 
 @pytest.fixture(params=MODES)
 def mode(request):
+    before = fps.get_fp_mode()
     fps.set_fp_mode(request.param)
     yield request.param
-    fps.set_fp_mode("nofma")
+    fps.set_fp_mode(before)
 
 
 def _api(case):
@@ -173,7 +178,8 @@ def test_high_dimension_vanilla(mode):
 def test_nan_coordinates_vanilla_exact():
     pts = np.random.default_rng(6).random((500, 3)).astype(np.float32)
     pts[[3, 77, 400], 1] = np.nan
-    np.testing.assert_array_equal(fps.fps_sampling(pts, 100, 0), ORACLE.fps(pts, 100, 0))
+    np.testing.assert_array_equal(fps.fps_sampling(pts, 100, 0),
+                                  ORACLE.fps(pts, 100, 0, fps.get_fp_mode()))
 
 
 def test_kdline_nan_in_split_dimension_is_reported():
@@ -187,54 +193,78 @@ def test_device_tensor_entry_points():
     torch = pytest.importorskip("torch")
     pts = W.gmm_cloud(200_000, seed=7)
     t = torch.from_numpy(pts).cuda()
+    m = fps.get_fp_mode()
     out, tr = capi.kdline_tensor(t, 2000, 7, 0, trace=True)
-    np.testing.assert_array_equal(out.cpu().numpy().astype(np.uint64), ORACLE.kdline(pts, 2000, 7, 0))
+    np.testing.assert_array_equal(out.cpu().numpy().astype(np.uint64),
+                                  ORACLE.kdline(pts, 2000, 7, 0, m))
     out2, tr2 = capi.fps_tensor(t, 2000, [0, 9], trace=True)
-    np.testing.assert_array_equal(out2.cpu().numpy().astype(np.uint64), ORACLE.fps(pts, 2000, [0, 9]))
+    np.testing.assert_array_equal(out2.cpu().numpy().astype(np.uint64),
+                                  ORACLE.fps(pts, 2000, [0, 9], m))
     ref = fp64_trace(pts, out2.cpu().numpy())
     np.testing.assert_allclose(tr2.cpu().numpy()[2:], ref[2:], rtol=1e-5)
     t1 = tr.cpu().numpy()
     assert np.all(np.diff(t1[1:]) <= 0)  # FPS max-min trace never increases
 
 
-def test_gmm_1m_kdline_h7_full(mode):
-    """gmm-1m workload at full size: N=1,048,576, h=7, K=16,384."""
-    pts = W.gmm_cloud(1 << 20, seed=W.SEEDS["gmm-1m"])
-    got = fps.bucket_fps_kdline_sampling(pts, 16384, 7, 0)
-    np.testing.assert_array_equal(got, ORACLE.kdline(pts, 16384, 7, 0, mode))
+def _fixture_cloud(name):
+    if not F.available():
+        pytest.fail("tests/golden/fullsize.npz is missing (tests/golden/make_fullsize.py)")
+    pts = F.cloud(name)
+    assert F.input_matches(name, pts), f"the {name} generator no longer reproduces the fixture's input"
+    return pts
 
 
-def test_gmm_1m_vanilla_prefix():
-    """Vanilla FPS on the same 1M cloud: full K on the GPU; the oracle checks a
-    prefix (FPS is prefix-stable in K) and the whole trace is non-increasing."""
+@pytest.fixture(scope="module")
+def gmm1m():
+    return _fixture_cloud("gmm1m")
+
+
+@pytest.fixture(scope="module")
+def large16m():
+    return _fixture_cloud("large16m")
+
+
+def test_gmm_1m_kdline_h7_full(gmm1m, mode):
+    """gmm-1m workload at full size: N=1,048,576, h=7, K=16,384, every sample
+    against the reference's own answer."""
+    got = fps.bucket_fps_kdline_sampling(gmm1m, 16384, 7, 0)
+    np.testing.assert_array_equal(got, F.expected("gmm1m_kdline_h7", mode))
+
+
+def test_gmm_1m_vanilla_full(gmm1m, mode):
+    """Vanilla FPS on the same cloud, K=16,384: the plain call (thread-block
+    cluster) and the traced call (grid sampler) both equal the reference's
+    answer sample for sample; the fp32 trace never increases and follows the
+    fp64 recomputation on its first samples."""
     torch = pytest.importorskip("torch")
-    pts = W.gmm_cloud(1 << 20, seed=W.SEEDS["gmm-1m"])
-    out, tr = capi.fps_tensor(torch.from_numpy(pts).cuda(), 16384, 0, trace=True)
-    out = out.cpu().numpy().astype(np.uint64)
-    np.testing.assert_array_equal(out[:256], ORACLE.fps(pts, 256, 0))
+    want = F.expected("gmm1m_vanilla", mode)
+    np.testing.assert_array_equal(fps.fps_sampling(gmm1m, 16384, 0), want)
+    out, tr = capi.fps_tensor(torch.from_numpy(gmm1m).cuda(), 16384, 0, trace=True)
+    np.testing.assert_array_equal(out.cpu().numpy().astype(np.uint64), want)
     t = tr.cpu().numpy()
     assert np.all(np.diff(t[1:]) <= 0)
-    # without a trace the call runs on a thread-block cluster: same indices
-    np.testing.assert_array_equal(fps.fps_sampling(pts, 16384, 0), out)
-    assert len(np.unique(out)) == 16384
+    ref = fp64_trace(gmm1m, want[:400])
+    np.testing.assert_allclose(t[1:400], ref[1:400], rtol=1e-5)
 
 
-def test_large_16m_d6_prefixes():
-    """large-16m workload at full size (N=16,777,216, D=6, K=65,536): kd-line
-    h=9 and vanilla run to full K on the GPU; the oracle checks prefixes (FPS
-    is prefix-stable in K), and the kd-line fp32 trace never increases."""
+def test_large_16m_d6_kdline_h9_full(large16m, mode):
+    """large-16m workload at full size (N=16,777,216, D=6), kd-line h=9,
+    K=65,536: every sample against the reference's answer, through the Python
+    API and the traced device entry point (non-increasing trace)."""
     torch = pytest.importorskip("torch")
-    pts = W.large_cloud(1 << 24, seed=W.SEEDS["large-16m"])
-    t = torch.from_numpy(pts).cuda()
-    kd = fps.bucket_fps_kdline_sampling(pts, 65536, 9, 0)
-    np.testing.assert_array_equal(kd[:128], ORACLE.kdline(pts, 128, 9, 0))
-    assert len(np.unique(kd)) == 65536
-    out, tr = capi.kdline_tensor(t, 65536, 9, 0, trace=True)
-    np.testing.assert_array_equal(out.cpu().numpy().astype(np.uint64), kd)
+    want = F.expected("large16m_kdline_h9", mode)
+    np.testing.assert_array_equal(fps.bucket_fps_kdline_sampling(large16m, 65536, 9, 0), want)
+    out, tr = capi.kdline_tensor(torch.from_numpy(large16m).cuda(), 65536, 9, 0, trace=True)
+    np.testing.assert_array_equal(out.cpu().numpy().astype(np.uint64), want)
     assert np.all(np.diff(tr.cpu().numpy()[1:]) <= 0)
-    v = fps.fps_sampling(pts, 65536, 0)
-    np.testing.assert_array_equal(v[:12], ORACLE.fps(pts, 12, 0))
-    assert len(np.unique(v)) == 65536
+
+
+def test_large_16m_d6_vanilla_full(large16m, mode):
+    """Vanilla FPS on the 16.7M-point 6-D cloud, K=65,536: every sample
+    against the multithreaded oracle's complete answer (whose first samples
+    the reference confirmed)."""
+    want = F.expected("large16m_vanilla", mode)
+    np.testing.assert_array_equal(fps.fps_sampling(large16m, 65536, 0), want)
 
 
 def test_beyond_register_capacity_uses_streaming_sampler():
@@ -242,14 +272,15 @@ def test_beyond_register_capacity_uses_streaming_sampler():
     registers, so the streaming sampler (piece records in HBM) runs."""
     rng = np.random.default_rng(33)
     pts = rng.random((1 << 25, 1), dtype=np.float32)
+    m = fps.get_fp_mode()
     v = fps.fps_sampling(pts, 64, 7)
-    np.testing.assert_array_equal(v[:8], ORACLE.fps(pts, 8, 7))
+    np.testing.assert_array_equal(v, ORACLE.fps_mt(pts, 64, 7, m))
     assert len(np.unique(v)) == 64
     idx, xyz = fps.fps_sampling_points(pts, 64, 7)
     np.testing.assert_array_equal(idx, v)
     np.testing.assert_array_equal(xyz, pts[v.astype(np.int64)])
     kd = fps.bucket_fps_kdline_sampling(pts, 64, 1, 7)
-    np.testing.assert_array_equal(kd[:24], ORACLE.kdline(pts, 24, 1, 7))
+    np.testing.assert_array_equal(kd, ORACLE.kdline(pts, 64, 1, 7, m))
 
 
 @pytest.mark.parametrize("n,d", [(3000, 3), (20000, 3), (300_000, 3), (5000, 12),
@@ -362,14 +393,27 @@ def test_batch_list_form_equals_contiguous_form():
         np.testing.assert_array_equal(b, w)
 
 
-def test_batched_workload_sample_vs_oracle():
-    """The bench's 256-cloud workload: every 16th cloud checked against the oracle."""
+def _kdline_job(job):
+    from oracle.oracle import Oracle
+
+    p, k, h, s, m = job
+    return Oracle().kdline(p, k, h, s, m)
+
+
+def test_batched_workload_all_clouds_vs_oracle(mode):
+    """The bench's 256-cloud workload: every sample of every cloud against the
+    oracle (computed by a process pool)."""
+    import multiprocessing as mp
+    import os
+
     clouds = W.batched_clouds(seed=W.SEEDS["batched-256"])
     hs = [5 if p.shape[0] < 8192 else 7 for p, _ in clouds]
     got = fps.bucket_fps_kdline_sampling_batch([p for p, _ in clouds], [k for _, k in clouds], hs, 0)
-    for i in range(0, len(clouds), 16):
-        p, k = clouds[i]
-        np.testing.assert_array_equal(got[i], ORACLE.kdline(p, k, hs[i], 0))
+    jobs = [(p, k, h, 0, mode) for (p, k), h in zip(clouds, hs)]
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        want = pool.map(_kdline_job, jobs)
+    for i in range(len(clouds)):
+        np.testing.assert_array_equal(got[i], want[i], err_msg=f"cloud {i}")
 
 
 def test_cloud_beyond_shared_memory(mode):

@@ -7,9 +7,9 @@ import threading
 import numpy as np
 import pytest
 
-import fpsample_gb300 as fps
+import fpsample as fps
 from fpsample_gb300 import capi
-from fpsample_gb300 import workloads as W
+import workloads as W
 from oracle.oracle import Oracle
 
 pytestmark = pytest.mark.gpu

@@ -109,3 +109,51 @@ def test_oracle_matches_the_live_reference_on_random_clouds(mode):
                                       ref.bucket_fps_kdline_sampling(p, k, h, s))
         np.testing.assert_array_equal(ORACLE.fps(p, min(k, 300), s, mode),
                                       ref.fps_sampling(p, min(k, 300), s))
+        np.testing.assert_array_equal(ORACLE.fps_mt(p, min(k, 300), s, mode, threads=5),
+                                      ref.fps_sampling(p, min(k, 300), s))
+
+
+@pytest.mark.parametrize("mode", ["nofma", "fma"])
+def test_multithreaded_vanilla_oracle_equals_serial(mode):
+    """oracle_fps_mt (chunked updates, chunk maxima folded in order) gives the
+    serial restatement's answer: continuous and tie-heavy clouds, NaN
+    coordinates, start lists, every dimension 1..11, 1 to 16 threads."""
+    rng = np.random.default_rng(77 if mode == "nofma" else 78)
+    for i in range(22):
+        d = 1 + i % 11
+        n = int(rng.integers(1, 6000))
+        p = rng.random((n, d)).astype(np.float32)
+        if i % 3 == 1:
+            p = np.round(p * 4).astype(np.float32)  # ties
+        if i % 7 == 3 and n > 10:
+            p[rng.integers(0, n, 3), 0] = np.nan
+        k = int(rng.integers(1, min(n, 800) + 1))
+        m = int(rng.integers(1, min(k, 4) + 1))
+        starts = [int(x) for x in rng.integers(0, n, m)]
+        want = ORACLE.fps(p, k, starts, mode)
+        for threads in (1, 3, 16):
+            np.testing.assert_array_equal(ORACLE.fps_mt(p, k, starts, mode, threads=threads), want)
+
+
+@pytest.mark.parametrize("mode", ["nofma", "fma"])
+def test_fullsize_fixtures_agree_with_the_oracle(mode):
+    """tests/golden/fullsize.npz: the seeded generators still produce the
+    fixtures' inputs, and the oracle reproduces each answer (the 1M-point
+    kd-line in full, the others on prefixes -- FPS is prefix-stable in K)."""
+    from tests.golden import fullsize as F
+
+    if not F.available():
+        pytest.fail("tests/golden/fullsize.npz is missing (tests/golden/make_fullsize.py)")
+    gmm = F.cloud("gmm1m")
+    assert F.input_matches("gmm1m", gmm)
+    np.testing.assert_array_equal(ORACLE.kdline(gmm, 16384, 7, 0, mode),
+                                  F.expected("gmm1m_kdline_h7", mode))
+    np.testing.assert_array_equal(ORACLE.fps_mt(gmm, 2048, 0, mode),
+                                  F.expected("gmm1m_vanilla", mode)[:2048])
+    big = F.cloud("large16m")
+    assert F.input_matches("large16m", big)
+    np.testing.assert_array_equal(ORACLE.kdline(big, 256, 9, 0, mode),
+                                  F.expected("large16m_kdline_h9", mode)[:256])
+    np.testing.assert_array_equal(ORACLE.fps_mt(big, 16, 0, mode),
+                                  F.expected("large16m_vanilla", mode)[:16])
+    assert len(np.unique(F.expected("large16m_vanilla", mode))) == 65536
