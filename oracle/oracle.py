@@ -23,6 +23,7 @@ from __future__ import annotations
 import ctypes
 import importlib.util
 import os
+import platform
 import subprocess
 import sys
 import sysconfig
@@ -33,7 +34,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 ROOT = os.path.dirname(HERE)
 REF_SRC = os.path.join(ROOT, "baseline", "_ref", "src", "fpsample")
-REF_FLAGS = os.path.join(HERE, "_ref", "flags.txt")
+# builds of the reference for this host's CPU architecture (oracle/Makefile ref)
+REF_OUT = os.path.join(HERE, "_ref", platform.machine())
+REF_FLAGS = os.path.join(REF_OUT, "flags.txt")
 
 FP_MODES = {"nofma": 0, "fma": 1}
 
@@ -201,7 +204,7 @@ def reference_build_flags(mode: str) -> str | None:
 
 def reference_available(mode: str = "nofma") -> bool:
     ext = sysconfig.get_config_var("EXT_SUFFIX")
-    return os.path.isdir(REF_SRC) and os.path.exists(os.path.join(HERE, "_ref", mode, "_fpsample" + ext))
+    return os.path.isdir(REF_SRC) and os.path.exists(os.path.join(REF_OUT, mode, "_fpsample" + ext))
 
 
 def load_reference(mode: str = "nofma"):
@@ -214,7 +217,7 @@ def load_reference(mode: str = "nofma"):
         return sys.modules[name]
     spec = importlib.util.spec_from_file_location(
         name, os.path.join(REF_SRC, "__init__.py"),
-        submodule_search_locations=[os.path.join(HERE, "_ref", mode), REF_SRC])
+        submodule_search_locations=[os.path.join(REF_OUT, mode), REF_SRC])
     mod = importlib.util.module_from_spec(spec)
     sys.modules[name] = mod
     spec.loader.exec_module(mod)

@@ -2,7 +2,10 @@
 
 Run where the reference sources are staged (``make -C oracle stage ref``):
 
-    python tests/golden/make_fullsize.py            # both FP modes, ~40 min
+    python tests/golden/make_fullsize.py [--cache DIR]   # both FP modes, ~30 min
+
+With --cache, every answer is also saved to DIR as it is computed and reused
+by the next run.
 
 Which answer comes from where:
 
@@ -21,7 +24,8 @@ Which answer comes from where:
                      smaller clouds
 
 "nofma" is the reference built without FMA contraction, "fma" the same
-sources with contraction (on x86-64: -mfma).  Indices are stored as uint32
+sources with contraction everywhere, as GCC compiles them on aarch64 (on
+x86-64: -mfma --param=avoid-fma-max-bits=0, see oracle/Makefile).  Indices are stored as uint32
 (every cloud has fewer than 2**32 points) beside the sha256 of the input the
 seeded generator produced, so a test can tell a changed generator from a
 wrong answer.
@@ -82,26 +86,54 @@ def _reference_job(job):
     return case, mode, np.asarray(out, np.uint64), time.perf_counter() - t0
 
 
+def _cached(cache, case, mode):
+    if cache and os.path.exists(os.path.join(cache, f"{case}__{mode}.npy")):
+        return np.load(os.path.join(cache, f"{case}__{mode}.npy"))
+    return None
+
+
+def _store(cache, case, mode, out):
+    if cache:
+        os.makedirs(cache, exist_ok=True)
+        np.save(os.path.join(cache, f"{case}__{mode}.npy"), out)
+
+
 def main() -> None:
+    import argparse
+
     from oracle.oracle import Oracle, load_reference, reference_build_flags
 
-    jobs = [(c, m) for c, v in CASES.items() if v[5] == "reference" for m in MODES]
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--cache", default=None)
+    cache = ap.parse_args().cache
+    results, seconds = {}, {}
+    for c in CASES:
+        for m in MODES:
+            got = _cached(cache, c, m)
+            if got is not None:
+                results[(c, m)], seconds[(c, m)] = got, None
+    jobs = [(c, m) for c, v in CASES.items() if v[5] == "reference" for m in MODES
+            if (c, m) not in results]
     # the reference is single-threaded: one process per run, the longest first
     jobs.sort(key=lambda j: -CASES[j[0]][2] * (1 << 20 if "16m" in j[0] else 1))
-    results, seconds = {}, {}
     t_all = time.perf_counter()
-    with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
-        for case, mode, out, dt in pool.imap_unordered(_reference_job, jobs):
-            results[(case, mode)] = out
-            seconds[(case, mode)] = dt
-            print(f"{case} {mode}: {dt:.0f} s (reference)", flush=True)
+    if jobs:
+        with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+            for case, mode, out, dt in pool.imap_unordered(_reference_job, jobs):
+                results[(case, mode)] = out
+                seconds[(case, mode)] = dt
+                _store(cache, case, mode, out)
+                print(f"{case} {mode}: {dt:.0f} s (reference)", flush=True)
     orc = Oracle()
     big = cloud("large16m")
     for mode in MODES:
+        if ("large16m_vanilla", mode) in results:
+            continue
         t0 = time.perf_counter()
         _, _, k, _, s, _ = CASES["large16m_vanilla"]
         results[("large16m_vanilla", mode)] = orc.fps_mt(big, k, s, mode)
         seconds[("large16m_vanilla", mode)] = time.perf_counter() - t0
+        _store(cache, "large16m_vanilla", mode, results[("large16m_vanilla", mode)])
         print(f"large16m_vanilla {mode}: {seconds[('large16m_vanilla', mode)]:.0f} s", flush=True)
 
     # cross-checks: the multithreaded oracle against the reference
@@ -127,7 +159,8 @@ def main() -> None:
             out = results[(case, mode)]
             assert out.shape == (k,) and int(out.max()) < 2**32
             arrays[f"{case}__{mode}"] = out.astype(np.uint32)
-            manifest["cases"][case]["seconds"][mode] = round(seconds[(case, mode)], 1)
+            sec = seconds[(case, mode)]
+            manifest["cases"][case]["seconds"][mode] = None if sec is None else round(sec, 1)
             if src == "reference":
                 manifest["cases"][case].setdefault("reference_flags", {})[mode] = \
                     reference_build_flags(mode)

@@ -148,8 +148,8 @@ def test_fullsize_fixtures_agree_with_the_oracle(mode):
     assert F.input_matches("gmm1m", gmm)
     np.testing.assert_array_equal(ORACLE.kdline(gmm, 16384, 7, 0, mode),
                                   F.expected("gmm1m_kdline_h7", mode))
-    np.testing.assert_array_equal(ORACLE.fps_mt(gmm, 2048, 0, mode),
-                                  F.expected("gmm1m_vanilla", mode)[:2048])
+    np.testing.assert_array_equal(ORACLE.fps_mt(gmm, 16384, 0, mode),
+                                  F.expected("gmm1m_vanilla", mode))
     big = F.cloud("large16m")
     assert F.input_matches("large16m", big)
     np.testing.assert_array_equal(ORACLE.kdline(big, 256, 9, 0, mode),
@@ -157,3 +157,18 @@ def test_fullsize_fixtures_agree_with_the_oracle(mode):
     np.testing.assert_array_equal(ORACLE.fps_mt(big, 16, 0, mode),
                                   F.expected("large16m_vanilla", mode)[:16])
     assert len(np.unique(F.expected("large16m_vanilla", mode))) == 65536
+
+
+def test_fullsize_fixtures_separate_the_fp_modes():
+    """At the benchmark sizes the two arithmetics pick different points, for
+    vanilla FPS as well as for the kd-line (the 1M-point vanilla cloud first
+    differs at sample 10691): the fma mode is exercised for both."""
+    from tests.golden import fullsize as F
+
+    if not F.available():
+        pytest.fail("tests/golden/fullsize.npz is missing (tests/golden/make_fullsize.py)")
+    for case in ("gmm1m_vanilla", "gmm1m_kdline_h7", "large16m_vanilla", "large16m_kdline_h9"):
+        a, b = F.expected(case, "nofma"), F.expected(case, "fma")
+        assert not np.array_equal(a, b), case
+    d = np.nonzero(F.expected("gmm1m_vanilla", "nofma") != F.expected("gmm1m_vanilla", "fma"))[0]
+    assert d[0] == 10691
