@@ -343,18 +343,82 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
-def _served_worker_init(folder):
+def _gen_points(job):
+    """Writes request i's cloud (from its own seed) to folder/i.npy."""
+    import workloads as W
+
+    i, n, seed, folder = job
+    np.save(os.path.join(folder, f"{i}.npy"), W.sphere_cloud(np.random.default_rng(seed), n))
+    return i
+
+
+def _scratch_dir():
+    return "/dev/shm" if os.path.isdir("/dev/shm") else None
+
+
+def served_requests(window_s: float):
+    """The first window_s seconds of the served stream (2000 requests/s)."""
+    import workloads as W
+
+    return list(W.request_stream(rate=2000.0, duration_s=window_s, seed=W.SEEDS["served"]))
+
+
+def admitted_requests(rho: float, samples_per_s: float):
+    """The whole 10 s stream thinned at random (a seeded coin per request) so
+    that the samples it offers per second are rho x samples_per_s: an admitted
+    load the server can sustain."""
+    import workloads as W
+
+    reqs = list(W.request_stream(rate=2000.0, duration_s=10.0, seed=W.SEEDS["served"]))
+    offered = sum(r.k for r in reqs) / 10.0
+    keep = min(1.0, rho * samples_per_s / offered)
+    coin = np.random.default_rng(W.SEEDS["served"] + 1000).random(len(reqs))
+    return [r for r, c in zip(reqs, coin) if c < keep], keep
+
+
+def materialize(reqs, folder):
+    """Every request's points, generated in parallel from the requests' seeds
+    (spawned processes, so this may run after CUDA is initialised)."""
+    import multiprocessing as mp
+
+    jobs = sorted(((i, r.n, r.seed, folder) for i, r in enumerate(reqs)), key=lambda j: -j[1])
+    with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
+        for _ in pool.imap_unordered(_gen_points, jobs):
+            pass
+    pts = []
+    for i in range(len(reqs)):
+        f = os.path.join(folder, f"{i}.npy")
+        pts.append(np.load(f))
+        os.unlink(f)
+    return pts
+
+
+def _served_worker_init():
     sys.path.insert(0, ROOT)
-    _W["folder"] = folder
     _W["impl"], _W["obj"] = _cpu_impl()
 
 
 def _served_worker_run(job):
-    i, k, h, s = job
-    pts = np.load(os.path.join(_W["folder"], f"{i}.npy"))
+    import workloads as W
+
+    i, n, seed, k, h, s = job
+    pts = W.sphere_cloud(np.random.default_rng(seed), n)
     t0 = time.perf_counter()
     _cpu_run(_W["impl"], _W["obj"], "kdline", pts, k, h, s)
     return i, time.perf_counter() - t0
+
+
+def _latency_summary(reqs, lat, queue, wall):
+    small = np.array([r.n <= 65536 for r in reqs])
+    pct = lambda x, q: float(np.percentile(x, q)) if len(x) else None
+    return {
+        "requests": len(reqs), "requests_per_s": len(reqs) / wall,
+        "samples_per_s": sum(r.k for r in reqs) / wall, "wall_s": wall,
+        "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max())},
+        "latency_ms_n_le_65536": {"p50": pct(lat[small], 50), "p99": pct(lat[small], 99),
+                                  "count": int(small.sum())},
+        "queue_ms": {"p50": pct(queue, 50), "p99": pct(queue, 99)},
+    }
 
 
 def run_served_reference(args):
@@ -370,51 +434,37 @@ def run_served_reference(args):
     import heapq
     import multiprocessing as mp
 
-    import workloads as W
-
-    reqs = [(r.arrival_s, r.points, r.k, h_for(r.points.shape[0]), r.start)
-            for r in W.request_stream(rate=2000.0, duration_s=args.served_window,
-                                      seed=W.SEEDS["served"])]
+    reqs = served_requests(args.served_window)
     impl, _ = _cpu_impl()
     cores = min(os.cpu_count() or 1, len(reqs))
-    with tempfile.TemporaryDirectory() as folder:
-        for i, (_, p, _, _, _) in enumerate(reqs):
-            np.save(os.path.join(folder, f"{i}.npy"), p)
-        jobs = sorted(((i, k, h, s) for i, (_, p, k, h, s) in enumerate(reqs)),
-                      key=lambda j: -reqs[j[0]][1].shape[0] * j[1])
-        with mp.get_context("spawn").Pool(cores, initializer=_served_worker_init,
-                                          initargs=(folder,)) as pool:
-            service = dict(pool.imap_unordered(_served_worker_run, jobs))
+    jobs = sorted(((i, r.n, r.seed, r.k, h_for(r.n), r.start) for i, r in enumerate(reqs)),
+                  key=lambda j: -j[1] * j[3])
+    with mp.get_context("spawn").Pool(cores, initializer=_served_worker_init) as pool:
+        service = dict(pool.imap_unordered(_served_worker_run, jobs))
     free = [0.0] * cores  # first come, first served on `cores` servers
     lat, queue = [], []
-    for i, (a, _, _, _, _) in enumerate(reqs):
+    for i, r in enumerate(reqs):
         t = heapq.heappop(free)
-        start = max(t, a)
+        start = max(t, r.arrival_s)
         done = start + service[i]
         heapq.heappush(free, done)
-        lat.append((done - a) * 1e3)
-        queue.append((start - a) * 1e3)
-    lat, queue = np.array(lat), np.array(queue)
+        lat.append((done - r.arrival_s) * 1e3)
+        queue.append((start - r.arrival_s) * 1e3)
     wall = max(free)
-    small = np.array([p.shape[0] <= 65536 for _, p, _, _, _ in reqs])
-    pct = lambda x, q: float(np.percentile(x, q)) if len(x) else None
-    v = len(reqs) / wall
+    summ = _latency_summary(reqs, np.array(lat), np.array(queue), wall)
+    v = summ["requests_per_s"]
     line = {
         "impl": "reference", "metric": "requests/sec (served)", "value": v, "unit": "requests/s",
         "n_gpus": 0, "higher_is_better": True, "data": "synthetic (seeded generators)",
         "config": {"workload": "served", "offered_rate_per_s": 2000, "window_s": args.served_window,
-                   "requests": len(reqs),
-                   "points_total": int(sum(p.shape[0] for _, p, _, _, _ in reqs)),
-                   "samples_total": int(sum(k for _, _, k, _, _ in reqs))},
-        "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max())},
-        "latency_ms_n_le_65536": {"p50": pct(lat[small], 50), "p99": pct(lat[small], 99),
-                                  "count": int(small.sum())},
-        "queue_ms": {"p50": pct(queue, 50), "p99": pct(queue, 99)},
-        "samples_per_s": sum(k for _, _, k, _, _ in reqs) / wall, "wall_s": wall,
+                   "requests": len(reqs), "points_total": int(sum(r.n for r in reqs)),
+                   "samples_total": int(sum(r.k for r in reqs)), "fp_mode": fp_mode()},
+        **{k: summ[k] for k in ("latency_ms", "latency_ms_n_le_65536", "queue_ms",
+                                "samples_per_s", "wall_s")},
         "cpu_baseline": {"value": v, "unit": "requests/s", "cores": cores, "kind": impl,
                          "sample": f"every request of the {args.served_window} s window timed once "
-                                   f"on {cores} processes, served first come first served by "
-                                   f"{cores} cores at the arrival times"},
+                                   f"on {cores} processes ({_cpu_describe(impl)}), served first "
+                                   f"come first served by {cores} cores at the arrival times"},
         "e2e": {"value": v, "unit": "requests/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -700,56 +750,82 @@ def run_gpu_arm(args):
         dist.destroy_process_group()
 
 
+def _replay(srv, reqs, pts):
+    """Submits every request at its arrival time (relative to now) and waits
+    for all results: (results, wall seconds)."""
+    tickets = [None] * len(reqs)
+    t0 = time.perf_counter()
+    for i, r in enumerate(reqs):
+        dt = t0 + r.arrival_s - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        tickets[i] = srv.submit(pts[i], r.k, h_for(r.n), r.start)
+    res = [srv.result(t) for t in tickets]
+    return res, time.perf_counter() - t0
+
+
 def run_served(args):
-    """The served workload: a Poisson stream of requests (2000/s) into the request server.
-    The first --served-window seconds of the 10 s stream are replayed at their
-    arrival times (the full stream would need ~80 GB of host memory for its
-    points).  Reports completed requests/s over the replay, the latency
-    percentiles (submit to result), and the same for requests of <= 65536
+    """The served workload: a Poisson stream of requests (2000/s) into the
+    request server, in two parts.
+
+      offered   the first --served-window seconds of the stream, replayed at
+                its arrival times: far more work than one GPU can do, so the
+                server runs saturated; completed samples/s over the replay is
+                the saturation throughput (requests wait in the queue, which
+                their latency shows);
+      admitted  the whole 10 s stream thinned at random to --served-load times
+                that saturation throughput, replayed the same way: latency at
+                a load the server sustains.
+
+    Every request's points come from its own seed and are generated on the
+    host cores before the replay.  Reports requests/s and samples/s, latency
+    percentiles (submit to result) overall and for requests of <= 65536
     points; a sample of results is compared with one call per cloud."""
-    import threading
+    import tempfile as tf
 
     from fpsample_gb300 import capi
-    import workloads as W
 
-    reqs = list(W.request_stream(rate=2000.0, duration_s=args.served_window,
-                                 seed=W.SEEDS["served"]))
-    reqs = [(r.arrival_s, r.points, r.k, h_for(r.points.shape[0]), r.start) for r in reqs]
+    reqs = served_requests(args.served_window)
+    with tf.TemporaryDirectory(dir=_scratch_dir()) as folder:
+        pts = materialize(reqs, folder)
     with capi.Server(150 << 30, small_workers=args.small_workers,
                      large_workers=args.large_workers) as srv:
-        for a, p, k, h, s in reqs[: min(8, len(reqs))]:  # warm-up (not timed)
-            srv.result(srv.submit(p, k, h, s))
-        tickets = [None] * len(reqs)
-        t0 = time.perf_counter()
-        for i, (a, p, k, h, s) in enumerate(reqs):
-            dt = t0 + a - time.perf_counter()
-            if dt > 0:
-                time.sleep(dt)
-            tickets[i] = srv.submit(p, k, h, s)
-        res = [srv.result(t) for t in tickets]
-        wall = time.perf_counter() - t0
-    lat = np.array([r[2] for r in res])
-    queue = np.array([r[1] for r in res])
-    small = np.array([p.shape[0] <= 65536 for _, p, _, _, _ in reqs])
-    check = list(range(0, len(reqs), max(1, len(reqs) // 8)))
-    same = all(np.array_equal(res[i][0], capi.bucket_fps_kdline(reqs[i][1], reqs[i][2],
-                                                                 reqs[i][4], reqs[i][3]))
-               for i in check)
-    pct = lambda x, q: float(np.percentile(x, q)) if len(x) else None
+        for i in range(min(8, len(reqs))):  # warm-up (not timed)
+            srv.result(srv.submit(pts[i], reqs[i].k, h_for(reqs[i].n), reqs[i].start))
+        res, wall = _replay(srv, reqs, pts)
+        offered = _latency_summary(reqs, np.array([r[2] for r in res]),
+                                   np.array([r[1] for r in res]), wall)
+        check = list(range(0, len(reqs), max(1, len(reqs) // 8)))
+        same = all(np.array_equal(res[i][0], capi.bucket_fps_kdline(pts[i], reqs[i].k,
+                                                                    reqs[i].start, h_for(reqs[i].n)))
+                   for i in check)
+        del pts, res
+        adm, keep = admitted_requests(args.served_load, offered["samples_per_s"])
+        with tf.TemporaryDirectory(dir=_scratch_dir()) as folder:
+            apts = materialize(adm, folder)
+        ares, awall = _replay(srv, adm, apts)
+        admitted = _latency_summary(adm, np.array([r[2] for r in ares]),
+                                    np.array([r[1] for r in ares]), awall)
+        acheck = list(range(0, len(adm), max(1, len(adm) // 8)))
+        same &= all(np.array_equal(ares[i][0], capi.bucket_fps_kdline(apts[i], adm[i].k,
+                                                                       adm[i].start, h_for(adm[i].n)))
+                    for i in acheck)
     line = {
-        "metric": "requests/sec (served)", "value": len(reqs) / wall, "unit": "requests/s",
+        "metric": "requests/sec (served)", "value": offered["requests_per_s"], "unit": "requests/s",
         "n_gpus": 1, "higher_is_better": True, "data": "synthetic (seeded generators)",
         "config": {"workload": "served", "offered_rate_per_s": 2000, "window_s": args.served_window,
-                   "requests": len(reqs), "points_total": int(sum(p.shape[0] for _, p, _, _, _ in reqs)),
-                   "samples_total": int(sum(k for _, _, k, _, _ in reqs)),
+                   "requests": len(reqs), "points_total": int(sum(r.n for r in reqs)),
+                   "samples_total": int(sum(r.k for r in reqs)),
                    "small_workers": args.small_workers, "large_workers": args.large_workers,
-                   "memory_budget_gb": 150},
-        "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max())},
-        "latency_ms_n_le_65536": {"p50": pct(lat[small], 50), "p99": pct(lat[small], 99),
-                                  "count": int(small.sum())},
-        "queue_ms": {"p50": pct(queue, 50), "p99": pct(queue, 99)},
-        "samples_per_s": sum(k for _, _, k, _, _ in reqs) / wall,
-        "wall_s": wall, "identical_to_single_calls": same, "checked": check,
+                   "memory_budget_gb": 150, "fp_mode": fp_mode()},
+        "offered": offered,
+        "saturation": {"samples_per_s": offered["samples_per_s"],
+                       "requests_per_s": offered["requests_per_s"]},
+        "admitted": dict(admitted, load_of_saturation=args.served_load, stream_s=10.0,
+                         kept_fraction=keep),
+        "latency_ms": admitted["latency_ms"],
+        "latency_ms_n_le_65536": admitted["latency_ms_n_le_65536"],
+        "identical_to_single_calls": same,
     }
     print(json.dumps(line), flush=True)
 
@@ -801,18 +877,125 @@ def run_latency_probe(args):
     print(json.dumps({"probe": "latency", "results": res}), flush=True)
 
 
+SAMPLER_CASES = {
+    # name: (what it runs, the kernel it is there for)
+    "resident-4k": ("vanilla FPS, 4,096 x 3 uniform, K=1,024", "vanilla_resident"),
+    "stream-400k-d12": ("vanilla FPS, 400,000 x 12 uniform, K=128", "vanilla_stream"),
+    "onecta-124k": ("kd-line h=7, 124,000 x 3 scaled box, K=31,000", "batch_sample (one CTA)"),
+    "cluster-gmm1m": ("kd-line h=7, the 1,048,576-point Gaussian mixture, K=4,096",
+                      "batch_sample (cluster), split_kernel exact levels"),
+    "gridsmem-200k": ("vanilla FPS with the fp32 trace, 200,000-point Gaussian mixture, K=2,000",
+                      "grid_sample_smem"),
+    "gridreg-8m-d6": ("vanilla FPS, 8,388,608 x 6 (the large cloud's generator), K=512",
+                      "grid_sample_reg"),
+    "stream-40m-d1": ("vanilla FPS, 41,943,040 x 1 uniform, K=64", "fps_sample"),
+}
+
+
+def run_sampler_probe(args):
+    """One call per sampler kind on a small seeded case, each timed alone
+    (CUDA events around the call, after one untimed call): the cases that the
+    ncu summaries under profiles/ capture one kernel of (ncu -k <kernel>
+    -c 1 python bench.py --probe samplers --case <name>)."""
+    import torch
+
+    import workloads as W
+    from fpsample_gb300 import capi
+
+    names = [args.case] if args.case else list(SAMPLER_CASES)
+    res = {}
+    for name in names:
+        if name == "resident-4k":
+            pts, call = W.uniform_cloud(4096, 3, seed=0), ("fps", 1024, 0)
+        elif name == "stream-400k-d12":
+            pts, call = W.uniform_cloud(400_000, 12, seed=5), ("fps", 128, 0)
+        elif name == "onecta-124k":
+            rng = np.random.default_rng(11)
+            pts = (rng.random((124_000, 3)) * rng.uniform(0.1, 10, 3)).astype(np.float32)
+            call = ("kdline", 31_000, 7)
+        elif name == "cluster-gmm1m":
+            pts, call = W.gmm_cloud(1 << 20, seed=W.SEEDS["gmm-1m"]), ("kdline", 4096, 7)
+        elif name == "gridsmem-200k":
+            pts, call = W.gmm_cloud(200_000, seed=7), ("fps-trace", 2000, 0)
+        elif name == "gridreg-8m-d6":
+            pts, call = W.large_cloud(1 << 23, seed=W.SEEDS["large-16m"]), ("fps", 512, 0)
+        elif name == "stream-40m-d1":
+            pts, call = W.uniform_cloud(40 << 20, 1, seed=6), ("fps", 64, 0)
+        else:
+            raise ValueError(name)
+        t = torch.from_numpy(pts).cuda()
+        kind, k, h = call
+        out = torch.empty(k, dtype=torch.int64, device="cuda")
+        tr = torch.empty(k, dtype=torch.float32, device="cuda")
+        s = torch.cuda.current_stream().cuda_stream
+
+        def once():
+            if kind == "kdline":
+                capi.kdline_device(t.data_ptr(), t.shape[0], t.shape[1], k, 0, h, out.data_ptr(), 0, s)
+            else:
+                capi.fps_device(t.data_ptr(), t.shape[0], t.shape[1], k, [0], out.data_ptr(),
+                                tr.data_ptr() if kind == "fps-trace" else 0, s)
+
+        once()
+        torch.cuda.synchronize()
+        capi.stats_reset()
+        capi.stats_timing(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        once()
+        e1.record()
+        torch.cuda.synchronize()
+        capi.stats_timing(False)
+        st = capi.stats()
+        res[name] = {"what": SAMPLER_CASES[name][0], "kernel": SAMPLER_CASES[name][1],
+                     "call_ms": e0.elapsed_time(e1), "sampler_ms": st["sampler_ms"],
+                     "samples": st["samples"], "boxes_tested": st["pieces_tested"],
+                     "distances_recomputed": st["points_touched"]}
+        del t
+    print(json.dumps({"probe": "samplers", "results": res}), flush=True)
+
+
+def _bench_peaks_lib():
+    """bench_peaks.cu compiled into _build/ (not part of the library)."""
+    import ctypes
+    import shutil
+
+    out_dir = os.path.join(ROOT, "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    so = os.path.join(out_dir, "libbenchpeaks.so")
+    src = os.path.join(ROOT, "bench_peaks.cu")
+    if not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(src):
+        nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+        nvcc = nvcc if os.path.exists(nvcc) else (shutil.which("nvcc") or "nvcc")
+        subprocess.run([nvcc, "-gencode=arch=compute_103a,code=sm_103a", "-O3", "-shared",
+                        "-Xcompiler", "-fPIC", "-o", so, src], check=True)
+    lib = ctypes.CDLL(so)
+    lib.bench_measure_bandwidth.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    lib.bench_measure_bandwidth.restype = ctypes.c_int
+    return lib
+
+
 def run_peaks_probe(args):
     """Shared-memory and L2 read bandwidth of this GPU (the roofline of vanilla
     FPS on clouds that stay on chip), best of five, beside the HBM copy
     bandwidth measured for this GPU type (MEASURED_PEAKS.json)."""
+    import ctypes
+
     import torch
 
-    from fpsample_gb300 import capi
-
     torch.cuda.init()
-    out = {"probe": "peaks", "device": torch.cuda.get_device_name(0)}
+    lib = _bench_peaks_lib()
+    out = {"probe": "peaks", "command": "python bench.py --probe peaks",
+           "device": torch.cuda.get_device_name(0)}
     for level, key in ((0, "smem_gbs"), (1, "l2_gbs")):
-        out[key] = max(capi.measure_bandwidth(level) for _ in range(5))
+        best = 0.0
+        for _ in range(5):
+            v = ctypes.c_double(0.0)
+            rc = lib.bench_measure_bandwidth(level, ctypes.byref(v))
+            if rc != 0:
+                raise RuntimeError(f"bench_measure_bandwidth({level}) failed: {rc}")
+            best = max(best, v.value)
+        out[key] = best
     try:
         out["hbm_gbs"] = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
     except (OSError, KeyError):
@@ -827,12 +1010,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched-256", choices=WORKLOADS)
-    ap.add_argument("--served-window", type=float, default=0.1,
-                    help="seconds of the served request stream to replay")
+    ap.add_argument("--served-window", type=float, default=1.0,
+                    help="seconds of the served request stream to replay at the offered rate")
+    ap.add_argument("--served-load", type=float, default=0.8,
+                    help="admitted load, as a fraction of the measured saturation throughput")
     ap.add_argument("--small-workers", type=int, default=8)
     ap.add_argument("--large-workers", type=int, default=2)
-    ap.add_argument("--probe", default=None, choices=["latency", "peaks"],
+    ap.add_argument("--probe", default=None, choices=["latency", "peaks", "samplers"],
                     help="print a diagnostic table instead of the benchmark line")
+    ap.add_argument("--case", default=None, choices=sorted(SAMPLER_CASES),
+                    help="with --probe samplers: run this case only")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -841,6 +1028,9 @@ def main():
         return
     if args.probe == "peaks":
         run_peaks_probe(args)
+        return
+    if args.probe == "samplers":
+        run_sampler_probe(args)
         return
     if args.workload == "served":
         run_served(args) if args.impl != "reference" else run_served_reference(args)

@@ -1,13 +1,17 @@
-// Bandwidth microbenchmarks for the roofline of the on-chip levels: aggregate
-// shared-memory read bandwidth and L2 read bandwidth of this GPU.  The vanilla
-// FPS configurations whose cloud stays on chip are bounded by these, not by
-// HBM; the measured HBM copy bandwidth of this GPU type covers the rest.  Diagnostics
-// only: nothing on the sampling path calls them.
+// Bandwidth microbenchmarks for bench.py's roofline of the on-chip levels:
+// aggregate shared-memory read bandwidth and L2 read bandwidth of this GPU.
+// The vanilla FPS configurations whose cloud stays on chip are bounded by
+// these, not by HBM; the measured HBM copy bandwidth of this GPU type covers
+// the rest.  Not part of the library: `bench.py --probe peaks` compiles this
+// file into a small shared object of its own and prints profiles/peaks.json.
 #include <cuda_runtime.h>
 
-#include "fpsgpu_internal.h"
+#define TRY(expr)                               \
+    do {                                        \
+        cudaError_t e_ = (expr);                \
+        if (e_ != cudaSuccess) return (int)e_;  \
+    } while (0)
 
-namespace fpsgpu {
 namespace {
 
 constexpr int kBwThreads = 1024;
@@ -51,46 +55,46 @@ __global__ void __launch_bounds__(kBwThreads) l2_read(const float4* __restrict__
 
 int measure(int level, double* gbs) {
     int dev = 0, sms = 0;
-    FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
-    FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    TRY(cudaGetDevice(&dev));
+    TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     float* sink = nullptr;
-    FPSGPU_CUDA_TRY(cudaMalloc(&sink, (size_t)sms * 8 * sizeof(float)));
+    TRY(cudaMalloc(&sink, (size_t)sms * 8 * sizeof(float)));
     cudaEvent_t e0, e1;
-    FPSGPU_CUDA_TRY(cudaEventCreate(&e0));
-    FPSGPU_CUDA_TRY(cudaEventCreate(&e1));
+    TRY(cudaEventCreate(&e0));
+    TRY(cudaEventCreate(&e1));
     double bytes = 0.0;
     float ms = 0.0f;
-    int rc = FPSGPU_OK;
+    int rc = 0;
     if (level == 0) {
         int per_sm = 0;
-        FPSGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, smem_read, kBwThreads, 0));
+        TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, smem_read, kBwThreads, 0));
         const int grid = sms * (per_sm > 0 ? per_sm : 1);
         const int iters = 1 << 14;
         smem_read<<<grid, kBwThreads>>>(iters, sink);  // warm-up
-        FPSGPU_CUDA_TRY(cudaEventRecord(e0));
+        TRY(cudaEventRecord(e0));
         smem_read<<<grid, kBwThreads>>>(iters, sink);
-        FPSGPU_CUDA_TRY(cudaEventRecord(e1));
+        TRY(cudaEventRecord(e1));
         bytes = (double)grid * kBwThreads * iters * sizeof(float4);
     } else if (level == 1) {
         const size_t n4 = (32ull << 20) / sizeof(float4);  // 32 MB: resident in L2
         float4* buf = nullptr;
-        FPSGPU_CUDA_TRY(cudaMalloc(&buf, n4 * sizeof(float4)));
-        FPSGPU_CUDA_TRY(cudaMemset(buf, 0, n4 * sizeof(float4)));
+        TRY(cudaMalloc(&buf, n4 * sizeof(float4)));
+        TRY(cudaMemset(buf, 0, n4 * sizeof(float4)));
         const int grid = sms * 2, passes = 64;
         l2_read<<<grid, kBwThreads>>>(buf, n4, 2, sink);  // warm-up, loads the buffer into L2
-        FPSGPU_CUDA_TRY(cudaEventRecord(e0));
+        TRY(cudaEventRecord(e0));
         l2_read<<<grid, kBwThreads>>>(buf, n4, passes, sink);
-        FPSGPU_CUDA_TRY(cudaEventRecord(e1));
+        TRY(cudaEventRecord(e1));
         bytes = (double)n4 * sizeof(float4) * passes;
-        FPSGPU_CUDA_TRY(cudaEventSynchronize(e1));
+        TRY(cudaEventSynchronize(e1));
         cudaFree(buf);
     } else {
-        rc = set_error(FPSGPU_ERR_ARG, "unknown bandwidth level %d (0 shared memory, 1 L2)", level);
+        rc = -1;  // unknown level (0 shared memory, 1 L2)
     }
     if (!rc) {
-        FPSGPU_CUDA_TRY(cudaGetLastError());
-        FPSGPU_CUDA_TRY(cudaEventSynchronize(e1));
-        FPSGPU_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        TRY(cudaGetLastError());
+        TRY(cudaEventSynchronize(e1));
+        TRY(cudaEventElapsedTime(&ms, e0, e1));
         *gbs = ms > 0.0f ? bytes / (ms * 1e-3) / 1e9 : 0.0;
     }
     cudaEventDestroy(e0);
@@ -100,10 +104,10 @@ int measure(int level, double* gbs) {
 }
 
 }  // namespace
-}  // namespace fpsgpu
 
-extern "C" int fpsgpu_measure_bandwidth(int level, double* gbs) {
-    fpsgpu::clear_error();
-    if (!gbs) return fpsgpu::set_error(FPSGPU_ERR_ARG, "null output");
-    return fpsgpu::measure(level, gbs);
+// Read bandwidth in GB/s of level 0 (shared memory, all SMs) or 1 (L2, a 32 MB
+// buffer); 0 on success, else a cudaError_t value (-1: unknown level).
+extern "C" int bench_measure_bandwidth(int level, double* gbs) {
+    if (!gbs) return -1;
+    return measure(level, gbs);
 }

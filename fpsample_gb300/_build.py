@@ -28,8 +28,7 @@ LIB = os.path.join(HERE, "libfpsgpu.so")
 EXT = os.path.join(ROOT, "fpsample", "_fpsample" + sysconfig.get_config_var("EXT_SUFFIX"))
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_UNITS = ["api", "vanilla_nofma", "vanilla_fma", "engine_nofma", "engine_fma", "noalloc", "server",
-            "peaks"]
+CU_UNITS = ["api", "vanilla_nofma", "vanilla_fma", "engine_nofma", "engine_fma", "noalloc", "server"]
 
 
 def _nvcc() -> str:

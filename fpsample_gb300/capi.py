@@ -47,7 +47,6 @@ SIGNATURES = {
     "fpsgpu_last_error": (ctypes.c_char_p, []),
     "fpsgpu_selftest_exchange_timeout": (ctypes.c_int, []),
     "fpsgpu_debug_fail_allocations": (None, [ctypes.c_longlong]),
-    "fpsgpu_measure_bandwidth": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "fpsgpu_sample_points": (ctypes.c_int, [ctypes.c_int, _f32p, _sz, _sz, _sz, _szp, _sz, _sz,
                                             _szp, _f32p]),
     "fpsgpu_sample_points_device": (ctypes.c_int, [ctypes.c_int, _vp, _sz, _sz, _sz, _szp, _sz,
@@ -342,13 +341,6 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
-
-
-def measure_bandwidth(level: int) -> float:
-    """Read bandwidth in GB/s of an on-chip level: 0 shared memory, 1 L2."""
-    v = ctypes.c_double(0.0)
-    _check("fpsgpu_measure_bandwidth", lib().fpsgpu_measure_bandwidth(level, ctypes.byref(v)))
-    return v.value
 
 
 ALGO_FPS, ALGO_KDLINE, ALGO_KDTREE = 0, 1, 2

@@ -61,12 +61,22 @@ struct Request {
     double t_submit = 0, t_admit = 0, t_done = 0;
     int rc = 0;
     bool done = false;
+    bool claimed = false;  // a caller is waiting on it (one waiter per ticket)
+};
+
+// What one worker thread runs on: its stream and its memory pool, both made by
+// fpsgpu_server_create so that a failure is reported there.
+struct WorkerRes {
+    int cls = 0;
+    cudaStream_t stream = nullptr;
+    cudaMemPool_t pool = nullptr;
 };
 
 }  // namespace
 
 struct Server {
     int device = 0;
+    std::vector<WorkerRes> res;
     size_t budget = 0, in_use = 0;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -78,31 +88,11 @@ struct Server {
     std::atomic<uint64_t> batches{0};
     int grid_cap = 0;  // CTAs a multi-CTA sampler may use, so batches can overlap
 
-    void worker(int cls) {
+    void worker(WorkerRes res) {
         cudaSetDevice(device);
-        cudaStream_t stream;
-        // small requests first: their streams get the device's highest priority,
-        // so their CTAs are scheduled ahead of the large class's as SMs free up
-        int lo_prio = 0, hi_prio = 0;
-        cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
-        if (cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking,
-                                         cls == 0 ? hi_prio : lo_prio) != cudaSuccess)
-            return;
-        // a memory pool of this worker's own: no allocation of this worker can
-        // be made to wait for another worker's batch
-        cudaMemPool_t pool = nullptr;
-        {
-            cudaMemPoolProps props = {};
-            props.allocType = cudaMemAllocationTypePinned;
-            props.location.type = cudaMemLocationTypeDevice;
-            props.location.id = device;
-            if (cudaMemPoolCreate(&pool, &props) == cudaSuccess) {
-                uint64_t keep = budget;  // keep freed memory for the next batch
-                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-            } else {
-                pool = nullptr;
-            }
-        }
+        const int cls = res.cls;
+        cudaStream_t stream = res.stream;
+        cudaMemPool_t pool = res.pool;
         set_thread_pool(pool);
         for (;;) {
             std::vector<Request*> batch;
@@ -202,10 +192,61 @@ struct Server {
         }
         cudaStreamSynchronize(stream);
         set_thread_pool(nullptr);
-        if (pool) cudaMemPoolDestroy(pool);
-        cudaStreamDestroy(stream);
     }
 };
+
+// Frees what make_worker_res made.
+void free_worker_res(std::vector<WorkerRes>& rs) {
+    for (WorkerRes& r : rs) {
+        if (r.stream) {
+            cudaStreamSynchronize(r.stream);
+            cudaStreamDestroy(r.stream);
+        }
+        if (r.pool) cudaMemPoolDestroy(r.pool);
+    }
+    rs.clear();
+}
+
+// One stream and one memory pool per worker.  Small requests first: their
+// streams get the device's highest priority, so their CTAs are scheduled ahead
+// of the large class's as SMs free up.  Each worker allocates from a pool of
+// its own, so no allocation of one worker waits for another worker's batch;
+// a pool keeps up to budget / n_workers of freed memory for its next batch, so
+// the server never holds more than the admitted requests' memory plus one
+// budget.
+int make_worker_res(int device, size_t budget, int small_workers, int large_workers,
+                    std::vector<WorkerRes>& out) {
+    int lo_prio = 0, hi_prio = 0;
+    FPSGPU_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
+    const int n = small_workers + large_workers;
+    for (int i = 0; i < n; ++i) {
+        WorkerRes r;
+        r.cls = i < small_workers ? 0 : 1;
+        out.push_back(r);
+        cudaError_t e = cudaStreamCreateWithPriority(&out.back().stream, cudaStreamNonBlocking,
+                                                     r.cls == 0 ? hi_prio : lo_prio);
+        if (e != cudaSuccess) {
+            out.back().stream = nullptr;
+            free_worker_res(out);
+            return set_error(FPSGPU_ERR_CUDA, "cannot create a worker stream: %s",
+                             cudaGetErrorString(e));
+        }
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        e = cudaMemPoolCreate(&out.back().pool, &props);
+        if (e != cudaSuccess) {
+            out.back().pool = nullptr;
+            free_worker_res(out);
+            return set_error(FPSGPU_ERR_CUDA, "cannot create a worker memory pool: %s",
+                             cudaGetErrorString(e));
+        }
+        uint64_t keep = budget / (uint64_t)n;
+        cudaMemPoolSetAttribute(out.back().pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    return FPSGPU_OK;
+}
 
 }  // namespace fpsgpu
 
@@ -227,9 +268,11 @@ int fpsgpu_server_create(size_t max_device_bytes, int small_workers, int large_w
     int sms = 0;
     FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     s->grid_cap = std::max(1, sms / (large_workers + 1));
-
-    for (int i = 0; i < small_workers; ++i) s->workers.emplace_back(&Server::worker, s, 0);
-    for (int i = 0; i < large_workers; ++i) s->workers.emplace_back(&Server::worker, s, 1);
+    if (int rc = fpsgpu::make_worker_res(dev, s->budget, small_workers, large_workers, s->res)) {
+        delete s;
+        return rc;
+    }
+    for (const fpsgpu::WorkerRes& r : s->res) s->workers.emplace_back(&Server::worker, s, r);
     *out = s;
     return FPSGPU_OK;
 }
@@ -273,6 +316,9 @@ int fpsgpu_server_wait(void* server, uint64_t ticket, double* queue_ms, double* 
     auto it = s->reqs.find(ticket);
     if (it == s->reqs.end()) return fpsgpu::set_error(FPSGPU_ERR_ARG, "unknown ticket");
     Request* r = it->second.get();
+    // one waiter per ticket: the waiter erases the request when it returns
+    if (r->claimed) return fpsgpu::set_error(FPSGPU_ERR_ARG, "ticket already waited on");
+    r->claimed = true;
     s->cv_done.wait(lk, [&] { return r->done; });
     const int rc = r->rc;
     if (queue_ms) *queue_ms = r->t_admit - r->t_submit;
@@ -292,6 +338,7 @@ int fpsgpu_server_destroy(void* server) {
     s->cv_work.notify_all();
     s->cv_done.notify_all();
     for (auto& t : s->workers) t.join();
+    fpsgpu::free_worker_res(s->res);
     delete s;
     return FPSGPU_OK;
 }

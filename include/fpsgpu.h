@@ -178,11 +178,17 @@ int fpsgpu_kdline_batch_device(const float *d_points, const size_t *h_offsets,
  * the process first uses CUDA (the default, 8, let a small batch wait behind
  * a large batch's kernel: p99 latency of clouds up to 64K points 533 ms
  * instead of 21 ms in one measurement).
- *   create : budget in bytes of device memory for admitted requests
+ *   create : budget in bytes of device memory for admitted requests; the
+ *            workers' streams and memory pools are made here (an error code if
+ *            any cannot be).  Freed memory kept for reuse is capped at one
+ *            budget over all workers, so the server holds at most the admitted
+ *            requests' memory plus one budget.
  *   submit : host buffers; `points` and `sampled_point_indices` must stay valid
  *            until fpsgpu_server_wait returns for the ticket
  *   wait   : blocks until the request is done; queue_ms = time until its
- *            batch started, total_ms = submit-to-result latency (either may be NULL)
+ *            batch started, total_ms = submit-to-result latency (either may be
+ *            NULL).  One waiter per ticket: a second wait on a ticket that is
+ *            being waited on returns FPSGPU_ERR_ARG.
  *   destroy: finishes the requests already submitted, then stops the workers
  */
 int fpsgpu_server_create(size_t max_device_bytes, int small_workers, int large_workers,
@@ -279,12 +285,6 @@ int fpsgpu_kdline_batch_points_device(const float *d_points, const size_t *h_off
                                       const size_t *h_start_idx, const size_t *h_height,
                                       uint64_t *d_out, float *d_out_points, void *stream);
 
-/* ---- diagnostics (no reference counterpart) -------------------------------
- * Read bandwidth of an on-chip level of the current GPU, in GB/s, measured by a
- * short microbenchmark: level 0 = shared memory (all SMs together), level 1 =
- * L2 (a 32 MB buffer).  The roofline of vanilla FPS on clouds that stay on
- * chip.  Synchronous; allocates and frees its own buffers. */
-int fpsgpu_measure_bandwidth(int level, double *gbs);
 
 #ifdef __cplusplus
 }

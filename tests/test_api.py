@@ -163,3 +163,25 @@ def test_batch_list_extension_checks_and_no_cpu_fallback():
         assert "fpsgpu_kdline_batch_list failed with error code 4" in str(e)
     else:
         assert out.shape == (2,)
+
+
+def test_importable_under_the_reference_module_path():
+    """`import fpsample` and `fpsample._fpsample` resolve to this build, with
+    every public and extension name the reference defines
+    (src/fpsample/__init__.py:209-217, src/lib.cpp:598-653)."""
+    import os
+
+    import fpsample
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    assert os.path.dirname(fpsample.__file__) == os.path.join(root, "fpsample")
+    assert _fpsample.__name__ == "fpsample._fpsample"
+    assert os.path.dirname(_fpsample.__file__) == os.path.join(root, "fpsample")
+    for name in ("fps_sampling", "fps_npdu_sampling", "fps_npdu_kdtree_sampling",
+                 "bucket_fps_kdtree_sampling", "bucket_fps_kdline_sampling", "__version__",
+                 "__doc__"):
+        assert hasattr(fpsample, name), name
+    for name in ("_fps_sampling", "_fps_npdu_sampling", "_fps_npdu_kdtree_sampling",
+                 "_bucket_fps_kdtree_sampling", "_bucket_fps_kdline_sampling", "__version__"):
+        assert hasattr(_fpsample, name), name
+    from fpsample import fps_sampling  # noqa: F401  (the form callers write)

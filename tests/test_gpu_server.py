@@ -63,3 +63,36 @@ def test_server_tight_memory_budget():
         results = [srv.result(t)[0] for t in tickets]
     for (p, k, h, s), idx in zip(reqs, results):
         np.testing.assert_array_equal(idx, capi.bucket_fps_kdline(p, k, s, h))
+
+
+def test_server_refuses_a_second_waiter_on_one_ticket():
+    # one waiter per ticket: of two threads waiting on the same ticket, the
+    # one that claims it gets the result and the other an argument error,
+    # instead of touching a request the first waiter frees
+    import ctypes
+
+    rng = np.random.default_rng(5)
+    pts = np.ascontiguousarray(W.sphere_cloud(rng, 300_000), np.float32)
+    out = np.empty(60_000, np.uint64)
+    with capi.Server(8 << 30, small_workers=1, large_workers=1) as srv:
+        t = ctypes.c_uint64(0)
+        rc = capi.lib().fpsgpu_server_submit(srv._h, pts.ctypes.data_as(capi._f32p), pts.shape[0],
+                                             3, out.size, 0, 9, out.ctypes.data_as(capi._szp),
+                                             ctypes.byref(t))
+        assert rc == 0
+        rcs = []
+        lock = threading.Lock()
+
+        def waiter():
+            rc = capi.lib().fpsgpu_server_wait(srv._h, t.value, None, None)
+            with lock:
+                rcs.append(rc)
+
+        ths = [threading.Thread(target=waiter) for _ in range(2)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+    # FPSGPU_ERR_ARG (3): ticket already waited on, or already gone
+    assert sorted(rcs) == [0, 3]
+    np.testing.assert_array_equal(out, capi.bucket_fps_kdline(pts, out.size, 0, 9))

@@ -79,7 +79,7 @@ def test_served_reference_arm_line():
     served, reported in the GPU served line's units."""
     env = dict(os.environ, PYTHONPATH=ROOT)
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
-                        "--workload", "served", "--served-window", "0.0015"],
+                        "--workload", "served", "--served-window", "0.0002"],
                        capture_output=True, text=True, env=env, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     line = json.loads(r.stdout.strip().splitlines()[-1])

@@ -72,15 +72,22 @@ def sphere_cloud(rng: np.random.Generator, n: int, n_spheres: int = 16, outlier_
 
 @dataclass
 class Request:
+    """One served request; its points come from its own seed, so a request
+    stream can be drawn without holding every cloud in memory."""
     arrival_s: float
-    points: np.ndarray
+    n: int
     k: int
     start: int
+    seed: int
+
+    def points(self) -> np.ndarray:
+        return sphere_cloud(np.random.default_rng(self.seed), self.n)
 
 
 def request_stream(rate: float = 2000.0, duration_s: float = 10.0, lo: int = 4096,
                    hi: int = 2097152, seed: int = 3, max_requests: int | None = None):
-    """Yield the served workload's requests in arrival order (points generated lazily)."""
+    """Yield the served workload's requests in arrival order (points are
+    generated by Request.points)."""
     rng = np.random.default_rng(seed)
     t = 0.0
     i = 0
@@ -91,7 +98,7 @@ def request_stream(rate: float = 2000.0, duration_s: float = 10.0, lo: int = 409
         n = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
         k = int(rng.integers(n // 16, n // 4 + 1))
         start = int(rng.integers(0, n))
-        yield Request(t, sphere_cloud(rng, n), k, start)
+        yield Request(t, n, k, start, int(rng.integers(0, 2**63)))
         i += 1
 
 
