@@ -881,6 +881,8 @@ SAMPLER_CASES = {
     # name: (what it runs, the kernel it is there for)
     "resident-4k": ("vanilla FPS, 4,096 x 3 uniform, K=1,024", "vanilla_resident"),
     "stream-400k-d12": ("vanilla FPS, 400,000 x 12 uniform, K=128", "vanilla_stream"),
+    "onecta-8k": ("kd-line h=5, 8,192 x 3 scaled box (held in shared memory), K=2,048",
+                  "batch_sample (one CTA, points in shared memory)"),
     "onecta-124k": ("kd-line h=7, 124,000 x 3 scaled box, K=31,000", "batch_sample (one CTA)"),
     "cluster-gmm1m": ("kd-line h=7, the 1,048,576-point Gaussian mixture, K=4,096",
                       "batch_sample (cluster), split_kernel exact levels"),
@@ -909,6 +911,10 @@ def run_sampler_probe(args):
             pts, call = W.uniform_cloud(4096, 3, seed=0), ("fps", 1024, 0)
         elif name == "stream-400k-d12":
             pts, call = W.uniform_cloud(400_000, 12, seed=5), ("fps", 128, 0)
+        elif name == "onecta-8k":
+            rng = np.random.default_rng(12)
+            pts = (rng.random((8192, 3)) * rng.uniform(0.1, 10, 3)).astype(np.float32)
+            call = ("kdline", 2048, 5)
         elif name == "onecta-124k":
             rng = np.random.default_rng(11)
             pts = (rng.random((124_000, 3)) * rng.uniform(0.1, 10, 3)).astype(np.float32)

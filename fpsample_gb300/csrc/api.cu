@@ -199,15 +199,6 @@ uint32_t cluster_min_pieces() {
     return v;
 }
 
-// The one-CTA batched sampler: batch_sample_pp (dirty pieces recomputed by the
-// whole CTA, the default) or, with FPSGPU_ONECTA_SAMPLER=warp, batch_sample
-// (each warp recomputes its own dirty pieces).  Read at every call, so a test
-// can run both on the same clouds.
-bool onecta_per_warp() {
-    const char* e = std::getenv("FPSGPU_ONECTA_SAMPLER");
-    return e && std::strcmp(e, "warp") == 0;
-}
-
 // How many clusters of `cl` CTAs of `func` can be resident at once (0: none).
 int cluster_capacity(const void* func, int cl, int block, size_t smem, int* out) {
     *out = 0;

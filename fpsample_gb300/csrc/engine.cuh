@@ -1202,291 +1202,6 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
     }
 }
 
-// ---- batched sampling: one CTA per cloud, dirty pieces spread over the CTA --
-//
-// The same queue, piece ownership (slot j of lane, warp holds the cloud's
-// piece j * T + lane * nwarps + warp, box and max key in registers), keys and
-// arithmetic as batch_sample<CL=false>; what changes is who recomputes a
-// dirty piece.  In batch_sample one warp recomputes each of its dirty pieces,
-// four points per lane, so a sample waits for the warp with the most dirty
-// work: measured on GB300, that warp's recompute is ~1000 cycles of a
-// ~2000-cycle sample on a shared-memory-resident cloud and ~2900 of ~4000 on a
-// 124K-point cloud in L2 (about two dirty pieces on the busiest warp).  Here a
-// sample is:
-//   P1  every thread tests its slots against r; each dirty slot takes an
-//       index in the CTA's dirty list (one shared atomicAdd per warp, the
-//       slots' ranks from ballots);                                  barrier
-//   P2  round after round, dirty pieces [8u, 8u + 8) (16 with 1024 threads) are
-//       recomputed by pairs of warps, a point per lane and pass (two passes
-//       for a 128-point piece, both loads issued first); each warp leaves its
-//       max key and the coordinates behind it in a candidate slot;   barrier
-//       the owner of each of those pieces takes the larger candidate as the
-//       piece's new key (register) and max coordinates (shared memory);
-//   P3  every thread's largest key -> warp max -> one word per warp; barrier;
-//       every warp reduces the warp maxima; the key names the winner's piece,
-//       whose max coordinates are the next r.
-// Candidate slots alternate between two buffers by round, so a round's
-// writes never meet the previous round's readers.  The first sample (every
-// piece dirty, running distances initialised) takes batch_sample's per-warp
-// recompute.  Results are identical to batch_sample's: the same keys are
-// computed and the same maxima taken, only on other threads.
-template <int D, bool FMA, bool KD>
-__global__ void __launch_bounds__(batch_threads(D), 1) batch_sample_pp(BatchArgs a) {
-    constexpr int kWarps = batch_threads(D) / 32;
-    constexpr int kGroups = kWarps / 2;  // pieces recomputed per round
-    extern __shared__ __align__(16) unsigned char s_dyn[];
-    __shared__ uint32_t s_item;
-    __shared__ uint32_t s_cnt[2];                   // dirty count, by sample parity
-    __shared__ uint32_t s_dlist[2048];              // dirty pieces (local index) of this sample
-    __shared__ uint64_t s_ck[2][kGroups][2];        // candidate keys [round buffer][group][warp]
-    __shared__ float s_cc[2][kGroups][2][D];        // and the coordinates behind them
-    __shared__ uint64_t s_wk[kWarps];               // per-warp maxima of the sample
-    const uint32_t cap = a.cap, mcap = a.mcap;
-    float* s_x = reinterpret_cast<float*>(s_dyn);                 // [D][mcap]
-    float* s_dis = s_x + (size_t)D * mcap;                        // [mcap]
-    uint32_t* s_tag = reinterpret_cast<uint32_t*>(s_dis + mcap);  // [mcap]
-    uint32_t* s_ps = s_tag + mcap;                                // [cap] my pieces' starts
-    uint32_t* s_pe = s_ps + cap;                                  // [cap] and ends
-    float* s_mc = reinterpret_cast<float*>(s_pe + cap);           // [D][cap] max coordinates
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t T = blockDim.x;
-    const int grp = warp >> 1, wg = warp & 1;
-    const uint32_t lt_mask = (1u << lane) - 1u;
-    const uint64_t n = a.n;
-    unsigned long long tested = 0, touched = 0;
-
-    for (;;) {
-        if (tid == 0) s_item = atomicAdd(a.queue, 1u);
-        __syncthreads();
-        const uint32_t item = s_item;
-        if (item >= a.n_items) break;
-        const uint32_t c = a.order[item];
-        const uint32_t P0 = a.cloud_piece[c];
-        const uint32_t np = a.cloud_piece[c + 1] - P0;
-        const uint64_t K = a.cloud_k[c];
-        const uint64_t coff = a.cloud_off[c];
-        const uint32_t nc = (uint32_t)(a.cloud_off[c + 1] - coff);
-        const uint64_t ooff = a.out_off[c];
-        const bool resident = nc <= mcap;
-
-        const uint32_t nmine = np;
-        const uint32_t ns = (nmine + T - 1) / T;  // slots in use by some thread
-        float lo[batch_slots(D)][D], hi[batch_slots(D)][D];
-        uint64_t key[batch_slots(D)];
-        uint32_t myq[batch_slots(D)], di[batch_slots(D)];
-#pragma unroll
-        for (int j = 0; j < batch_slots(D); ++j) {
-            myq[j] = (uint32_t)j * T + (uint32_t)lane * kWarps + warp;
-            key[j] = 0;
-            di[j] = ~0u;
-            const bool have = myq[j] < nmine;
-            const uint64_t q = (uint64_t)P0 + myq[j];
-#pragma unroll
-            for (int d = 0; d < D; ++d) {
-                lo[j][d] = have ? a.plo[q * D + d] : INFINITY;
-                hi[j][d] = have ? a.phi[q * D + d] : -INFINITY;
-            }
-        }
-        for (uint32_t i = tid; i < nmine; i += T) {
-            const uint64_t q = (uint64_t)P0 + i;
-            s_ps[i] = a.pstart[q] - (uint32_t)coff;
-            s_pe[i] = a.pstart[q + 1] - (uint32_t)coff;
-        }
-        if (resident) {
-            for (uint32_t i = tid; i < nc; i += T) {
-#pragma unroll
-                for (int d = 0; d < D; ++d) s_x[(size_t)d * mcap + i] = a.X[(uint64_t)d * n + coff + i];
-                s_tag[i] = a.tag[coff + i];
-            }
-        }
-        const float* xb = resident ? s_x : a.X + coff;
-        const uint64_t xs = resident ? mcap : n;
-        float* disb = resident ? s_dis : a.dis + coff;
-        const uint32_t* tagb = resident ? s_tag : a.tag + coff;
-        const uint32_t tag0 = (uint32_t)a.cloud_tag0[c];
-        float r[D];
-#pragma unroll
-        for (int d = 0; d < D; ++d) r[d] = a.Xref[(uint64_t)d * n + tag0];
-        if (tid == 0 && K > 0) a.out[ooff] = KD ? tag0 : tag0 - coff;
-        if (a.out_pts && K > 0) {
-#pragma unroll
-            for (int d = 0; d < D; ++d)
-                if (tid == d) a.out_pts[ooff * D + d] = r[d];
-        }
-        if (tid < 2) s_cnt[tid] = 0u;
-        __syncthreads();
-        {
-            uint32_t mine = 0;
-#pragma unroll
-            for (int j = 0; j < batch_slots(D); ++j) mine += myq[j] < nmine ? 1u : 0u;
-            if (K > 2) tested += (unsigned long long)mine * (K - 2);
-        }
-
-        for (uint64_t t = 0; t + 1 < K; ++t) {
-            const int cpar = (int)(t & 1);
-            if (t == 0) {
-                // first sample: every held piece, each by its own warp, running
-                // distances initialised to min(init, d)
-#pragma unroll
-                for (int j = 0; j < batch_slots(D); ++j) {
-                    if ((uint32_t)j >= ns) break;
-                    uint32_t m = __ballot_sync(kFull, myq[j] < nmine);
-                    while (m) {
-                        const int l = __ffs(m) - 1;
-                        m &= m - 1;
-                        const uint32_t q = __shfl_sync(kFull, myq[j], l);
-                        const uint32_t ps = s_ps[q], pe = s_pe[q];
-                        if (lane == 0) touched += pe - ps;
-                        const uint64_t wk = recompute_piece<D, FMA, KD>(
-                            xb, xs, disb, tagb, ps, pe, r, true, s_mc + q, cap, (uint32_t)coff, q);
-                        if (lane == l) key[j] = wk;
-                    }
-                }
-            } else {
-                // P1: box tests; dirty slots into the dirty list
-                uint32_t dm = 0;
-#pragma unroll
-                for (int j = 0; j < batch_slots(D); ++j) {
-                    if ((uint32_t)j < ns) {  // CTA-uniform
-                        const bool dj = box_bound<D, FMA>(lo[j], hi[j], r) < key_dist(key[j]);
-                        dm |= (uint32_t)dj << j;
-                    }
-                }
-                uint32_t bal[batch_slots(D)];
-                uint32_t cnt = 0;
-#pragma unroll
-                for (int j = 0; j < batch_slots(D); ++j) {
-                    bal[j] = (uint32_t)j < ns ? __ballot_sync(kFull, (dm >> j) & 1u) : 0u;
-                    cnt += __popc(bal[j]);
-                }
-                if (cnt) {
-                    uint32_t base = 0;
-                    if (lane == 0) base = atomicAdd(&s_cnt[cpar], cnt);
-                    base = __shfl_sync(kFull, base, 0);
-#pragma unroll
-                    for (int j = 0; j < batch_slots(D); ++j) {
-                        if ((dm >> j) & 1u) {
-                            di[j] = base + __popc(bal[j] & lt_mask);
-                            s_dlist[di[j]] = myq[j];
-                        }
-                        base += __popc(bal[j]);
-                    }
-                }
-                __syncthreads();
-                const uint32_t nd = s_cnt[cpar];
-                if (tid == 0) s_cnt[cpar ^ 1] = 0u;  // next sample's count (read last before this sample)
-                // P2: rounds of kGroups dirty pieces
-                for (uint32_t r0 = 0; r0 < nd; r0 += kGroups) {
-                    const int cb = (int)((r0 / kGroups) & 1);
-                    const uint32_t i = r0 + (uint32_t)grp;
-                    if (i < nd) {
-                        const uint32_t q = s_dlist[i];
-                        const uint32_t ps = s_ps[q], pe = s_pe[q];
-                        if (wg == 0 && lane == 0) touched += pe - ps;
-                        uint64_t pk = 0;
-                        float pc[D];
-#pragma unroll
-                        for (int d = 0; d < D; ++d) pc[d] = 0.0f;
-                        for (uint32_t p0 = ps + (uint32_t)wg * 32 + lane; p0 < pe; p0 += 128) {
-                            const uint32_t p1 = p0 + 64;
-                            const bool h1 = p1 < pe;
-                            float x0[D], x1[D];
-#pragma unroll
-                            for (int d = 0; d < D; ++d) {
-                                x0[d] = xb[(uint64_t)d * xs + p0];
-                                x1[d] = h1 ? xb[(uint64_t)d * xs + p1] : 0.0f;
-                            }
-                            const float o0 = disb[p0], o1 = h1 ? disb[p1] : 0.0f;
-                            const uint32_t g0 = tagb[p0], g1 = h1 ? tagb[p1] : 0u;
-                            const float d0 = sqdist<D, FMA>(x0, r);
-                            float v0 = o0;
-                            if (d0 < v0) {
-                                v0 = d0;
-                                disb[p0] = v0;
-                            }
-                            const uint64_t k0 = batch_key<KD>(v0, g0 - (uint32_t)coff, q);
-                            if (k0 > pk) {
-                                pk = k0;
-#pragma unroll
-                                for (int d = 0; d < D; ++d) pc[d] = x0[d];
-                            }
-                            if (h1) {
-                                const float d1 = sqdist<D, FMA>(x1, r);
-                                float v1 = o1;
-                                if (d1 < v1) {
-                                    v1 = d1;
-                                    disb[p1] = v1;
-                                }
-                                const uint64_t k1 = batch_key<KD>(v1, g1 - (uint32_t)coff, q);
-                                if (k1 > pk) {
-                                    pk = k1;
-#pragma unroll
-                                    for (int d = 0; d < D; ++d) pc[d] = x1[d];
-                                }
-                            }
-                        }
-                        const uint64_t wk = warp_max_key(pk);
-                        if (lane == 0) s_ck[cb][grp][wg] = wk;
-                        if (pk == wk && wk != 0) {
-#pragma unroll
-                            for (int d = 0; d < D; ++d) s_cc[cb][grp][wg][d] = pc[d];
-                        }
-                    }
-                    __syncthreads();
-                    // owners of this round's pieces take the larger candidate
-#pragma unroll
-                    for (int j = 0; j < batch_slots(D); ++j) {
-                        if (di[j] - r0 < (uint32_t)kGroups) {
-                            const uint32_t g = di[j] - r0;
-                            const uint64_t c0 = s_ck[cb][g][0], c1 = s_ck[cb][g][1];
-                            const int w = c1 > c0 ? 1 : 0;
-                            key[j] = w ? c1 : c0;
-#pragma unroll
-                            for (int d = 0; d < D; ++d) s_mc[(size_t)d * cap + myq[j]] = s_cc[cb][g][w][d];
-                            di[j] = ~0u;
-                        }
-                    }
-                }
-            }
-            // P3: the CTA's max key; its piece's max coordinates are the next r
-            uint64_t lbest = 0;
-#pragma unroll
-            for (int j = 0; j < batch_slots(D); ++j) lbest = key[j] > lbest ? key[j] : lbest;
-            const uint64_t wbest = warp_max_key(lbest);
-            if (lane == 0) s_wk[warp] = wbest;
-            __syncthreads();
-            const uint64_t g = warp_max_key(lane < kWarps ? s_wk[lane] : 0ull);
-            const uint32_t qw = (uint32_t)g & ((1u << kBatchPieceBits) - 1);
-#pragma unroll
-            for (int d = 0; d < D; ++d) r[d] = s_mc[(size_t)d * cap + qw];
-            if (tid == 0) {
-                const uint32_t loc = batch_key_pos<KD>(g);
-                a.out[ooff + t + 1] = KD ? loc + (uint32_t)coff : loc;
-            }
-            if (a.out_pts) {  // the winner's coordinates are the new r
-#pragma unroll
-                for (int d = 0; d < D; ++d)
-                    if (tid == 32 + d) a.out_pts[(ooff + t + 1) * D + d] = r[d];
-            }
-        }
-        __syncthreads();  // thread 0's output writes are visible to the CTA
-        if (KD) {
-            for (uint64_t i = tid; i < K; i += T) a.out[ooff + i] = a.idmap[a.out[ooff + i]] - coff;
-        }
-    }
-    if (a.counters) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            tested += __shfl_xor_sync(kFull, tested, o);
-            touched += __shfl_xor_sync(kFull, touched, o);
-        }
-        if (lane == 0) {
-            atomicAdd(a.counters, tested);
-            atomicAdd(a.counters + 1, touched);
-        }
-    }
-}
-
 // ---- one cloud on the whole grid, piece records in registers ----------------
 //
 // For clouds whose points fit neither one SM nor a cluster (e.g. 16.7M points):
@@ -2417,19 +2132,11 @@ int run_batch(const BatchCall& bc) {
     int dev = 0, smem_optin = 0;
     FPSGPU_CUDA_TRY(cudaGetDevice(&dev));
     FPSGPU_CUDA_TRY(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const bool per_warp = onecta_per_warp();
-    const void* one_kern =
-        per_warp ? (bc.kd ? (const void*)batch_sample<D, FMA, true, false>
-                          : (const void*)batch_sample<D, FMA, false, false>)
-                 : (bc.kd ? (const void*)batch_sample_pp<D, FMA, true>
-                          : (const void*)batch_sample_pp<D, FMA, false>);
     size_t static_smem = 0;
     {
         cudaFuncAttributes fa{};
-        FPSGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, one_kern));
+        FPSGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)batch_sample<D, FMA, true, false>));
         static_smem = fa.sharedSizeBytes;
-        FPSGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)batch_sample<D, FMA, true, true>));
-        static_smem = std::max<size_t>(static_smem, fa.sharedSizeBytes);
     }
     const size_t avail = (size_t)smem_optin - static_smem - 256;
     const uint32_t cap_max = (uint32_t)batch_slots(D) * batch_threads(D);
@@ -2569,7 +2276,8 @@ int run_batch(const BatchCall& bc) {
             const size_t left = avail - batch_smem_bytes(D, cap, 0);
             a.mcap = (uint32_t)std::min<uint64_t>(left / (4 * D + 8), max_nc);
             const size_t smem = batch_smem_bytes(D, cap, a.mcap);
-            const void* kern = one_kern;
+            const void* kern = bc.kd ? (const void*)batch_sample<D, FMA, true, false>
+                                     : (const void*)batch_sample<D, FMA, false, false>;
             if (int arc = allow_max_smem((const void*)kern)) return arc;
             int per_sm = 0;
             FPSGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, batch_threads(D), smem));

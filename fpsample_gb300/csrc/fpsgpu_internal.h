@@ -173,7 +173,6 @@ int allow_cluster16(const void* func);
 int cluster_size_for_batch();
 bool cluster_size_fixed();
 uint32_t cluster_min_pieces();
-bool onecta_per_warp();
 int cluster_capacity(const void* func, int cl, int block, size_t smem, int* out);
 int launch_clustered(const void* func, int items, int cl, int block, void** args, size_t smem,
                      cudaStream_t stream, int max_ctas = 0);

@@ -449,22 +449,3 @@ def test_batch_with_several_cluster_clouds(d, mode):
     got = capi.kdline_batch(clouds, ks, hs, ss)
     for p, k, h, s, g in zip(clouds, ks, hs, ss, got):
         np.testing.assert_array_equal(g, ORACLE.kdline(p, k, h, s, mode))
-
-
-@pytest.mark.parametrize("sampler", ["pp", "warp"])
-@pytest.mark.parametrize("d", [1, 3, 6])
-def test_both_one_cta_samplers_equal_the_oracle(sampler, d, mode, monkeypatch):
-    """The one-CTA batched sampler exists in two forms: dirty pieces recomputed
-    by the whole CTA (default) and by their own warp (FPSGPU_ONECTA_SAMPLER=warp).
-    Both must give the oracle's answer, on clouds that stay in shared memory and
-    on clouds read from L2, with ties."""
-    if sampler == "warp":
-        monkeypatch.setenv("FPSGPU_ONECTA_SAMPLER", "warp")
-    clouds, ks, hs, ss = _batch_clouds(50 + d, 10, 200, 120_000, d)
-    got = capi.kdline_batch(clouds, ks, hs, ss)
-    for p, k, h, s, g in zip(clouds, ks, hs, ss, got):
-        np.testing.assert_array_equal(g, ORACLE.kdline(p, k, h, s, mode))
-    # single-start vanilla takes the same engine
-    p = clouds[-1]
-    np.testing.assert_array_equal(fps.fps_sampling(p, min(2000, p.shape[0]), 3),
-                                  ORACLE.fps(p, min(2000, p.shape[0]), 3, mode))
