@@ -10,14 +10,21 @@ tree height picked per size class.  One step = all 256 clouds sampled.
           point), L2 flushed before each step, timed with CUDA events on the
           launching stream; max over ranks.
   e2e     clouds/s through the public drop-in API from host numpy arrays
-          (fpsample_gb300.bucket_fps_kdline_sampling), host<->device copies
-          inside the timed region.
-  roofline  the sampling kernel: algorithmic bytes per launch (bounding boxes
-          tested x (8D+8) B + running distances recomputed x (4D+8) B, both
-          counted on the device) / its event-timed average launch duration,
-          against the measured HBM copy bandwidth.
-  cpu_baseline  the oracle (C restatement of the reference, or the reference
-          compiled from its sources where present) on a bounded sample, 1 core.
+          (fpsample.bucket_fps_kdline_sampling / fps_sampling), host<->device
+          copies inside the timed region; one-cloud workloads add where the
+          end-to-end time goes (e2e_phases).
+  roofline  the sampling kernel: algorithmic bytes per launch -- kd-line:
+          sum over clouds of 2^h (8D+8) (K-1) B of bucket records plus the
+          running distances recomputed (device counter) x (4D+8) B; vanilla:
+          N (K-1) (4D+8) B -- over its event-timed average launch duration,
+          against the measured HBM copy bandwidth (frac), and the measured L2
+          and shared-memory read bandwidths (frac_l2, frac_smem); actual_* are
+          the bytes the pruned sampler really touches.
+  bit_exact  every sample of every cloud of the timed step against the
+          reference's answer: the full-size fixtures (tests/golden/fullsize.npz)
+          for the one-cloud benchmark sizes, else the oracle.
+  cpu_baseline  the reference compiled from its own sources on this host (the
+          oracle port where that build is absent) on a bounded sample, 1 core.
 
 Other workloads (--workload), each one of the reference's configurations:
   gmm-1m            one 1,048,576-point Gaussian-mixture cloud, kd-line h=7,
@@ -27,14 +34,14 @@ Other workloads (--workload), each one of the reference's configurations:
   large-16m         16,777,216 points, D=6, kd-line h=9, K=65,536
   large-16m-vanilla the same cloud, vanilla FPS
   served            a Poisson request stream into the request server
-Where the oracle cannot finish a cloud in seconds, the correctness check
-compares a prefix of the samples (FPS is prefix-stable in K) and the CPU
-numbers come from two truncated runs extrapolated linearly in K (said so in
-the line).
+Where the reference cannot finish a cloud in seconds (the 1M-point vanilla
+and 16.7M-point clouds), the CPU numbers come from two truncated runs
+extrapolated linearly in K (said so in the line).
 
 --impl reference runs the reference's CPU implementation of the same path on
 all host cores (rank 0 only) and prints the same metric.  The reference is
-single-threaded per cloud, so a one-cloud workload uses one core.
+single-threaded per cloud, so a one-cloud workload uses one core.  Both arms
+use the floating-point mode of the host's stock reference build.
 Multi-GPU (torchrun): replicas only -- every rank samples its own copy of the
 batch; value = all clouds / max step time over ranks ("weak" scaling).
 """
@@ -699,6 +706,29 @@ def run_gpu_arm(args):
     barrier()
     e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world, dev)
     e2e_v = job_value(len(clouds), world, e2e_s)
+    # where the end-to-end time goes beyond the device step: the host->device
+    # copy of the same host arrays (pageable numpy memory, as the public API
+    # receives them) and the indices back, each timed alone
+    phases = None
+    if len(clouds) == 1:
+        ht = []
+        for _ in range(e2e_steps):
+            barrier()
+            t1 = time.perf_counter()
+            tmp = torch.from_numpy(pcs[0]).to(dev)
+            torch.cuda.synchronize()
+            ht.append(time.perf_counter() - t1)
+            del tmp
+        dt = []
+        for _ in range(e2e_steps):
+            barrier()
+            t1 = time.perf_counter()
+            d_out.cpu()
+            dt.append(time.perf_counter() - t1)
+        phases = {"e2e_ms": e2e_s * 1e3, "device_step_ms": ms,
+                  "h2d_pageable_ms": min(ht) * 1e3, "h2d_bytes": int(pcs[0].nbytes),
+                  "h2d_gbs": pcs[0].nbytes / min(ht) / 1e9, "d2h_ms": min(dt) * 1e3,
+                  "rest_ms": e2e_s * 1e3 - ms - min(ht) * 1e3 - min(dt) * 1e3}
 
     # the plain one-call-per-cloud GPU form on the same data, for comparison
     barrier()
@@ -734,6 +764,7 @@ def run_gpu_arm(args):
             "plain_per_cloud": {"value": len(clouds) / (plain_ms / 1e3), "unit": UNIT,
                                 "ms_per_step": plain_ms, "identical_to_batched": plain_ok,
                                 "batched_speedup": plain_ms / ms},
+            "e2e_phases": phases,
             "e2e": {"value": e2e_v, "unit": UNIT,
                     "h2d_bytes_per_step": int(host_all.nbytes),
                     "d2h_bytes_per_step": int(koffs[-1]) * 8},
