@@ -167,6 +167,14 @@ cudaMemPool_t thread_pool() {
 // Cluster size of the batched engine's cluster sampler: FPSGPU_CLUSTER_SIZE
 // (1 turns clusters off; 2, 4, 8 or 16), default 8; clouds that need more CTAs
 // get the next power of two up to 16.
+bool lead_sampler_enabled() {
+    static const bool v = [] {
+        const char* e = std::getenv("FPSGPU_ONECTA_SAMPLER");
+        return !(e && std::strcmp(e, "lockstep") == 0);
+    }();
+    return v;
+}
+
 int cluster_size_for_batch() {
     static const int v = [] {
         const char* e = std::getenv("FPSGPU_CLUSTER_SIZE");

@@ -1202,6 +1202,8 @@ __global__ void __launch_bounds__(batch_threads(D), 1) batch_sample(BatchArgs a)
     }
 }
 
+#include "lead_sample.cuh"
+
 // ---- one cloud on the whole grid, piece records in registers ----------------
 //
 // For clouds whose points fit neither one SM nor a cluster (e.g. 16.7M points):
@@ -2099,6 +2101,76 @@ struct BatchCall {
     int min_cluster = 0;
 };
 
+// The one-CTA clouds of a batched call (D <= 3) on lead_sample: float4 point
+// records and low key words for the whole call, then one persistent launch
+// over the clouds in `small` (beside the clusters, which hold `cl` CTAs each,
+// when both kinds run).
+template <int D, bool FMA>
+int launch_lead_sampler(const BatchCall& bc, const Built& bt, const std::vector<uint32_t>& small,
+                        const std::vector<uint32_t>& clustered, const uint32_t* d_order, unsigned int* d_queue,
+                        const uint64_t* d_coff, const uint32_t* d_cpiece, const uint64_t* d_k,
+                        const uint64_t* d_tag0, const uint64_t* d_ooff, unsigned long long* cnt, bool both,
+                        int cl, int maxc, int smem_optin, Scratch& sc) {
+    const size_t C = bc.off.size() - 1;
+    const uint64_t n = bc.off[C];
+    int rc;
+    float4* P4;
+    uint32_t* LW;
+    if ((rc = sc.alloc(&P4, n))) return rc;
+    if ((rc = sc.alloc(&LW, n))) return rc;
+    {
+        const int blocks = std::max(1, std::min(bc.sms * 8, (int)((n / 64 + 7) / 8)));
+        stats_count_launch();
+        if (bc.kd)
+            lead_prepare<D, true><<<blocks, 256, 0, bc.stream>>>(bt.X, bt.tag, n, bt.pstart, d_cpiece, d_coff,
+                                                                (uint32_t)C, P4, LW);
+        else
+            lead_prepare<D, false><<<blocks, 256, 0, bc.stream>>>(bt.X, bt.tag, n, bt.pstart, d_cpiece, d_coff,
+                                                                 (uint32_t)C, P4, LW);
+        FPSGPU_CUDA_TRY(cudaGetLastError());
+    }
+    const void* kern = bc.kd ? (const void*)lead_sample<D, FMA, true> : (const void*)lead_sample<D, FMA, false>;
+    size_t static_smem = 0;
+    {
+        cudaFuncAttributes fa{};
+        FPSGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, kern));
+        static_smem = fa.sharedSizeBytes;
+    }
+    if (static_smem + kLeadSmemBytes + 256 > (size_t)smem_optin)
+        return set_error(FPSGPU_ERR_CUDA, "lead_sample needs %zu bytes of shared memory, the device offers %d",
+                         static_smem + kLeadSmemBytes, smem_optin);
+    LeadArgs la{};
+    la.P4 = P4;
+    la.LW = LW;
+    la.pstart = bt.pstart;
+    la.plo = bt.plo;
+    la.phi = bt.phi;
+    la.cloud_piece = d_cpiece;
+    la.cloud_off = d_coff;
+    la.cloud_k = d_k;
+    la.cloud_tag0 = d_tag0;
+    la.out_off = d_ooff;
+    la.order = d_order;
+    la.n_items = (uint32_t)small.size();
+    la.n = n;
+    la.Xref = bt.Xref;
+    la.idmap = bc.kd ? bt.idsnap : nullptr;
+    la.out = bc.d_out;
+    la.queue = d_queue;
+    la.counters = cnt;
+    la.err = bt.err;
+    la.out_pts = bc.d_out_pts;
+    const size_t smem = kLeadSmemBytes;
+    if (int arc = allow_max_smem(kern)) return arc;
+    int per_sm = 0;
+    FPSGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kLeadThreads, smem));
+    int slots = std::max(1, per_sm) * bc.sms;
+    if (both) slots = std::max(1, slots - cl * std::min<int>((int)clustered.size(), maxc));
+    const int G = (int)std::min<uint64_t>(small.size(), (uint64_t)slots);
+    void* args[] = {&la};
+    return launch_persistent(kern, G, kLeadThreads, args, smem, bc.stream, false);
+}
+
 template <int D, bool FMA>
 int run_batch(const BatchCall& bc) {
     Scratch sc(bc.stream);
@@ -2140,6 +2212,9 @@ int run_batch(const BatchCall& bc) {
     }
     const size_t avail = (size_t)smem_optin - static_smem - 256;
     const uint32_t cap_max = (uint32_t)batch_slots(D) * batch_threads(D);
+    // one-CTA clouds of D <= 3 take the leader/worker sampler (lead_sample)
+    const bool use_lead = D <= 3 && lead_sampler_enabled();
+    const uint32_t one_cap = use_lead ? kLeadCap : cap_max;
     const int want_cluster = bc.min_cluster > 0 ? bc.min_cluster : cluster_size_for_batch();
     const uint32_t promote = cluster_min_pieces();
     std::vector<uint64_t> out_off(C), tag0(C);
@@ -2158,7 +2233,7 @@ int run_batch(const BatchCall& bc) {
         if (bc.k[c] == 0) continue;
         const bool to_cluster = cluster_size_for_batch() > 1 && np <= (uint64_t)kMaxCluster * cap_max &&
                                 nc <= kBatchMaxCloudPoints;
-        if (np <= cap_max && !(to_cluster && promote > 0 && np >= promote)) {
+        if (np <= one_cap && !(to_cluster && promote > 0 && np >= promote)) {
             small.push_back((uint32_t)c);
             cap = std::max(cap, np);
         } else if (to_cluster) {
@@ -2191,7 +2266,7 @@ int run_batch(const BatchCall& bc) {
         if (maxc < 1) {  // no such cluster on this device: the other samplers take them
             for (uint32_t c : clustered) {
                 const uint32_t np = h_cpiece[c + 1] - h_cpiece[c];
-                if (np <= cap_max) {
+                if (np <= one_cap) {
                     small.push_back(c);
                     cap = std::max(cap, np);
                 } else {
@@ -2264,7 +2339,14 @@ int run_batch(const BatchCall& bc) {
                                        cl_smem, both ? side.s : bc.stream, bc.sms)))
                 return rc;
         }
-        if (!small.empty()) {
+        if (!small.empty() && use_lead) {
+            if constexpr (D <= 3) {
+                if ((rc = launch_lead_sampler<D, FMA>(bc, bt, small, clustered, d_order, d_queue, d_coff,
+                                                      d_cpiece, d_k, d_tag0, d_ooff, cnt, both, cl, maxc,
+                                                      smem_optin, sc)))
+                    return rc;
+            }
+        } else if (!small.empty()) {
             a.order = d_order;
             a.n_items = (uint32_t)small.size();
             a.queue = d_queue;

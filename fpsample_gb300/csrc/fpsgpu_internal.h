@@ -171,6 +171,9 @@ int allow_cluster16(const void* func);
 
 // thread-block cluster launches (batched engine's cluster sampler)
 int cluster_size_for_batch();
+// One-CTA batched clouds of D <= 3 take the leader/worker sampler unless
+// FPSGPU_ONECTA_SAMPLER=lockstep selects the lockstep one (batch_sample).
+bool lead_sampler_enabled();
 bool cluster_size_fixed();
 uint32_t cluster_min_pieces();
 int cluster_capacity(const void* func, int cl, int block, size_t smem, int* out);
