@@ -372,12 +372,15 @@ __device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, fl
         }
         // ---- the new hot set: my kLeadHotPerWarp pieces of largest key
         uint32_t picked = 0;
+        uint64_t fk[kLeadSlots];  // every slot's key, for the picks
+#pragma unroll
+        for (int j = 0; j < kLeadSlots; ++j) fk[j] = full_key(j);
         for (int i = 0; i < kLeadHotPerWarp; ++i) {
             uint64_t lk = 0;
             int lj = 0;
 #pragma unroll
             for (int j = 0; j < kLeadSlots; ++j) {
-                const uint64_t kj = ((picked >> j) & 1u) ? 0ull : full_key(j);
+                const uint64_t kj = ((picked >> j) & 1u) ? 0ull : fk[j];
                 if (kj > lk) {
                     lk = kj;
                     lj = j;
@@ -458,21 +461,32 @@ __device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, fl
             hent = ne;
         }
         __syncwarp();
-        // copy the new entries in: all their records in one pass, padded to
-        // kPiece with the last record, low words in leader format; the record
-        // whose key is the piece's key gives the entry its leader key
-        for (uint32_t t = lane; t < nfill * kPiece; t += 32) {
-            const uint32_t f = S.fill[w][t / kPiece];
+        // copy the new entries in, padded to kPiece with the last record, low
+        // words in leader format (every load of an entry issued before the
+        // first use: one round trip per entry); the record whose key is the
+        // piece's key gives the entry its leader key
+        for (uint32_t fi = 0; fi < nfill; ++fi) {
+            const uint32_t f = S.fill[w][fi];
+            const uint64_t fkey = S.fkey[w][fi];
             const uint32_t e = f >> 26, ps = (f >> 8) & kLeadPosMask, len = f & 0xffu;
-            const uint32_t i = t % kPiece, ri = i < len ? i : len - 1;
-            const float4 x = gP[ps + ri];
-            const uint32_t lw = gL[ps + ri];
-            const uint32_t ll = lead_pos_leader<KD>(lead_loc_worker<KD>(lw)) | (ri << 6) | e;
-            s_pt[e * kPiece + i] = x;
-            s_lw[e * kPiece + i] = ll;
-            const uint64_t kk = ((uint64_t)(__float_as_uint(x.w) | 0x80000000u) << 32) | lw;
-            if (i < len && kk == S.fkey[w][t / kPiece]) S.hkey[e] = (kk & 0xffffffff00000000ull) | ll;
-            if (i == 0) {
+            float4 x[kPiece / 32];
+            uint32_t lw[kPiece / 32];
+#pragma unroll
+            for (int j = 0; j < kPiece / 32; ++j) {
+                const uint32_t i = lane + 32 * j, ri = i < len ? i : len - 1;
+                x[j] = gP[ps + ri];
+                lw[j] = gL[ps + ri];
+            }
+#pragma unroll
+            for (int j = 0; j < kPiece / 32; ++j) {
+                const uint32_t i = lane + 32 * j, ri = i < len ? i : len - 1;
+                const uint32_t ll = lead_pos_leader<KD>(lead_loc_worker<KD>(lw[j])) | (ri << 6) | e;
+                s_pt[e * kPiece + i] = x[j];
+                s_lw[e * kPiece + i] = ll;
+                const uint64_t kk = ((uint64_t)(__float_as_uint(x[j].w) | 0x80000000u) << 32) | lw[j];
+                if (i < len && kk == fkey) S.hkey[e] = (kk & 0xffffffff00000000ull) | ll;
+            }
+            if (lane == 0) {
                 S.hlen[e] = len;
                 S.hps[e] = ps;
                 S.hmod[e] = 0;
@@ -557,62 +571,65 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
         const float lo1[3] = {l1.x, l1.y, l1.z}, hi1[3] = {h1.x, h1.y, h1.z};
         bool mod0 = false, mod1 = false;
         uint32_t s = 0;
+        uint64_t wk = warp_max_key(k0 > k1 ? k0 : k1);  // the best hot key (warp-uniform)
         while (emitted < cc.K && s < (uint32_t)kLeadRefs) {
-            const uint64_t lk = k0 > k1 ? k0 : k1;
-            const uint64_t wk = warp_max_key(lk);
             if (wk <= Tb) break;
             const uint32_t e = (uint32_t)wk & 63u, rec = ((uint32_t)wk >> 6) & 127u;
             const float4 r = s_pt[e * kPiece + rec];
             if (lane == 0) {
-                const uint32_t loc = lead_loc_leader<KD>((uint32_t)wk);
-                S.outq[s] = loc;
+                S.outq[s] = lead_loc_leader<KD>((uint32_t)wk);
                 S.ref[s] = r;
                 st_release_cta_shared(&S.nref, s + 1);
-            }
-            ++emitted;
-            ++s;
-            // the winner's entry: always dirty (its max point is r)
-            {
-                const uint64_t nk = lead_update_hot<D, FMA>(s_pt + e * kPiece, s_lw + e * kPiece, r);
-                if (lane == (e & 31u)) {
-                    if (e < 32) {
-                        k0 = nk;
-                        mod0 = true;
-                    } else {
-                        k1 = nk;
-                        mod1 = true;
-                    }
-                }
-            }
-            // every other hot entry whose box is nearer than its key
-            const float rv[3] = {r.x, r.y, r.z};
-            const bool d0 = k0 != 0 && lane != e && box_bound<D, FMA>(lo0, hi0, rv) < key_dist(k0);
-            const bool d1 = k1 != 0 && lane + 32 != e && box_bound<D, FMA>(lo1, hi1, rv) < key_dist(k1);
-            if (lane == 0) {
                 tested += kLeadHot;
                 touched += kPiece;
             }
-            uint32_t m = __ballot_sync(kFull, d0);
-            while (m) {
-                const uint32_t l = __ffs(m) - 1;
-                m &= m - 1;
-                if (lane == 0) touched += kPiece;
-                const uint64_t nk = lead_update_hot<D, FMA>(s_pt + l * kPiece, s_lw + l * kPiece, r);
-                if (lane == l) {
-                    k0 = nk;
-                    mod0 = true;
-                }
+            ++emitted;
+            ++s;
+            // The other entries do not depend on the winner's recompute: their
+            // max and their box tests go first, so that they overlap it.
+            const bool o0 = lane != e, o1 = lane + 32 != e;
+            const uint64_t x0 = o0 ? k0 : 0ull, x1 = o1 ? k1 : 0ull;
+            const uint64_t om = warp_max_key(x0 > x1 ? x0 : x1);
+            const float rv[3] = {r.x, r.y, r.z};
+            const bool d0 = x0 != 0 && box_bound<D, FMA>(lo0, hi0, rv) < key_dist(x0);
+            const bool d1 = x1 != 0 && box_bound<D, FMA>(lo1, hi1, rv) < key_dist(x1);
+            // the winner's entry: always dirty (its max point is r)
+            const uint64_t nk = lead_update_hot<D, FMA>(s_pt + e * kPiece, s_lw + e * kPiece, r);
+            if (!o0) {
+                k0 = nk;
+                mod0 = true;
             }
-            m = __ballot_sync(kFull, d1);
-            while (m) {
-                const uint32_t l = __ffs(m) - 1;
-                m &= m - 1;
-                if (lane == 0) touched += kPiece;
-                const uint64_t nk = lead_update_hot<D, FMA>(s_pt + (l + 32) * kPiece, s_lw + (l + 32) * kPiece, r);
-                if (lane == l) {
-                    k1 = nk;
-                    mod1 = true;
+            if (!o1) {
+                k1 = nk;
+                mod1 = true;
+            }
+            if (__any_sync(kFull, d0 || d1)) {
+                // every other hot entry whose box is nearer than its key
+                uint32_t m = __ballot_sync(kFull, d0);
+                while (m) {
+                    const uint32_t l = __ffs(m) - 1;
+                    m &= m - 1;
+                    if (lane == 0) touched += kPiece;
+                    const uint64_t k = lead_update_hot<D, FMA>(s_pt + l * kPiece, s_lw + l * kPiece, r);
+                    if (lane == l) {
+                        k0 = k;
+                        mod0 = true;
+                    }
                 }
+                m = __ballot_sync(kFull, d1);
+                while (m) {
+                    const uint32_t l = __ffs(m) - 1;
+                    m &= m - 1;
+                    if (lane == 0) touched += kPiece;
+                    const uint64_t k = lead_update_hot<D, FMA>(s_pt + (l + 32) * kPiece, s_lw + (l + 32) * kPiece, r);
+                    if (lane == l) {
+                        k1 = k;
+                        mod1 = true;
+                    }
+                }
+                wk = warp_max_key(k0 > k1 ? k0 : k1);
+            } else {
+                wk = om > nk ? om : nk;  // nothing else changed
             }
             __syncwarp();  // the lowered distances are visible to every lane
         }
