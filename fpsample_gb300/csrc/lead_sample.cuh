@@ -575,41 +575,69 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
         while (emitted < cc.K && s < (uint32_t)kLeadRefs) {
             if (wk <= Tb) break;
             const uint32_t e = (uint32_t)wk & 63u, rec = ((uint32_t)wk >> 6) & 127u;
-            const float4 r = s_pt[e * kPiece + rec];
-            if (lane == 0) {
-                S.outq[s] = lead_loc_leader<KD>((uint32_t)wk);
-                S.ref[s] = r;
-                st_release_cta_shared(&S.nref, s + 1);
-                tested += kLeadHot;
-                touched += kPiece;
+            float4* const ep = s_pt + e * kPiece;
+            const uint32_t* const el = s_lw + e * kPiece;
+            const float4 r = ep[rec];
+            // the winner's entry is always dirty (its max point is r): its
+            // loads go first, everything else below overlaps them
+            float4 v[kPiece / 32];
+            uint32_t w[kPiece / 32];
+#pragma unroll
+            for (int j = 0; j < kPiece / 32; ++j) {
+                v[j] = ep[lane + 32 * j];
+                w[j] = el[lane + 32 * j];
             }
+            // publish (every lane stores the same values: no branch)
+            S.outq[s] = lead_loc_leader<KD>((uint32_t)wk);
+            S.ref[s] = r;
+            st_release_cta_shared(&S.nref, s + 1);
+            tested += lane == 0 ? kLeadHot : 0u;
+            touched += lane == 0 ? kPiece : 0u;
             ++emitted;
             ++s;
-            // The other entries do not depend on the winner's recompute: their
-            // max and their box tests go first, so that they overlap it.
+            // the other entries' box tests do not depend on the winner's
+            // recompute (branch-free, so they share its basic block)
             const bool o0 = lane != e, o1 = lane + 32 != e;
             const uint64_t x0 = o0 ? k0 : 0ull, x1 = o1 ? k1 : 0ull;
-            const uint64_t om = warp_max_key(x0 > x1 ? x0 : x1);
             const float rv[3] = {r.x, r.y, r.z};
-            const bool d0 = x0 != 0 && box_bound<D, FMA>(lo0, hi0, rv) < key_dist(x0);
-            const bool d1 = x1 != 0 && box_bound<D, FMA>(lo1, hi1, rv) < key_dist(x1);
-            // the winner's entry: always dirty (its max point is r)
-            const uint64_t nk = lead_update_hot<D, FMA>(s_pt + e * kPiece, s_lw + e * kPiece, r);
-            if (!o0) {
-                k0 = nk;
-                mod0 = true;
+            const bool d0 = (x0 != 0) & (box_bound<D, FMA>(lo0, hi0, rv) < key_dist(x0));
+            const bool d1 = (x1 != 0) & (box_bound<D, FMA>(lo1, hi1, rv) < key_dist(x1));
+            // the winner's recompute
+            uint32_t bh[kPiece / 32];
+#pragma unroll
+            for (int j = 0; j < kPiece / 32; ++j) {
+                const float dd = sqdist4<D, FMA>(v[j], r);
+                const bool lower = dd < v[j].w;
+                const float nv = lower ? dd : v[j].w;
+                if (lower) reinterpret_cast<float*>(ep + lane + 32 * j)[3] = nv;
+                bh[j] = __float_as_uint(nv) | 0x80000000u;
             }
-            if (!o1) {
-                k1 = nk;
-                mod1 = true;
-            }
+            lead_pmax(bh[0], w[0], bh[1], w[1]);
+            lead_pmax(bh[2], w[2], bh[3], w[3]);
+            lead_pmax(bh[0], w[0], bh[2], w[2]);
+            // One warp max over (the other entries' keys, this lane's best
+            // record of the winner's entry) gives the next winner; an
+            // independent one gives the winner entry's new key.  Their
+            // reductions issue side by side.
+            uint32_t ch = (uint32_t)(x0 >> 32), cl = (uint32_t)x0;
+            lead_pmax(ch, cl, (uint32_t)(x1 >> 32), (uint32_t)x1);
+            lead_pmax(ch, cl, bh[0], w[0]);
+            const uint32_t ah = __reduce_max_sync(kFull, ch);
+            const uint32_t nh = __reduce_max_sync(kFull, bh[0]);
+            const uint32_t al = __reduce_max_sync(kFull, ch == ah ? cl : 0u);
+            const uint32_t nl = __reduce_max_sync(kFull, bh[0] == nh ? w[0] : 0u);
+            const uint64_t nk = ((uint64_t)nh << 32) | nl;
+            k0 = o0 ? k0 : nk;
+            k1 = o1 ? k1 : nk;
+            mod0 |= !o0;
+            mod1 |= !o1;
             if (__any_sync(kFull, d0 || d1)) {
                 // every other hot entry whose box is nearer than its key
                 uint32_t m = __ballot_sync(kFull, d0);
                 while (m) {
                     const uint32_t l = __ffs(m) - 1;
                     m &= m - 1;
-                    if (lane == 0) touched += kPiece;
+                    touched += lane == 0 ? kPiece : 0u;
                     const uint64_t k = lead_update_hot<D, FMA>(s_pt + l * kPiece, s_lw + l * kPiece, r);
                     if (lane == l) {
                         k0 = k;
@@ -620,7 +648,7 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
                 while (m) {
                     const uint32_t l = __ffs(m) - 1;
                     m &= m - 1;
-                    if (lane == 0) touched += kPiece;
+                    touched += lane == 0 ? kPiece : 0u;
                     const uint64_t k = lead_update_hot<D, FMA>(s_pt + (l + 32) * kPiece, s_lw + (l + 32) * kPiece, r);
                     if (lane == l) {
                         k1 = k;
@@ -629,7 +657,7 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
                 }
                 wk = warp_max_key(k0 > k1 ? k0 : k1);
             } else {
-                wk = om > nk ? om : nk;  // nothing else changed
+                wk = ((uint64_t)ah << 32) | al;  // nothing else changed
             }
             __syncwarp();  // the lowered distances are visible to every lane
         }
