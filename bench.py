@@ -912,9 +912,10 @@ SAMPLER_CASES = {
     # name: (what it runs, the kernel it is there for)
     "resident-4k": ("vanilla FPS, 4,096 x 3 uniform, K=1,024", "vanilla_resident"),
     "stream-400k-d12": ("vanilla FPS, 400,000 x 12 uniform, K=128", "vanilla_stream"),
-    "onecta-8k": ("kd-line h=5, 8,192 x 3 scaled box (held in shared memory), K=2,048",
-                  "batch_sample (one CTA, points in shared memory)"),
-    "onecta-124k": ("kd-line h=7, 124,000 x 3 scaled box, K=31,000", "batch_sample (one CTA)"),
+    "onecta-8k": ("kd-line h=5, 8,192 x 3 scaled box, K=2,048",
+                  "lead_sample (one CTA: leader warp and worker warps)"),
+    "onecta-124k": ("kd-line h=7, 124,000 x 3 scaled box, K=31,000",
+                    "lead_sample (one CTA: leader warp and worker warps)"),
     "cluster-gmm1m": ("kd-line h=7, the 1,048,576-point Gaussian mixture, K=4,096",
                       "batch_sample (cluster), split_kernel exact levels"),
     "gridsmem-200k": ("vanilla FPS with the fp32 trace, 200,000-point Gaussian mixture, K=2,000",

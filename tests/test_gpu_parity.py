@@ -357,6 +357,29 @@ def test_batch_equals_oracle_per_cloud(seed, d, mode):
         np.testing.assert_array_equal(g, ORACLE.kdline(p, k, h, s, mode))
 
 
+@pytest.mark.parametrize("kind", ["kdline", "vanilla"])
+def test_one_cta_sampler_epochs_with_ties(kind, mode):
+    """Clouds of D <= 3 that one CTA samples with a hot table and many epochs,
+    on a coarse lattice (many equal distances, some repeated points: ties
+    decided by position, also between a hot piece and the workers' bound);
+    every sample against the oracle."""
+    rng = np.random.default_rng(21)
+    cases = []
+    for n, d in ((9000, 3), (40000, 3), (30000, 2), (20000, 1)):
+        p = (np.round(rng.random((n, d)) * 40) / 4).astype(np.float32)  # 0.25 lattice
+        cases.append((p, n // 4, 7, int(rng.integers(0, n))))
+    if kind == "kdline":
+        for d in (3, 2, 1):
+            sub = [c for c in cases if c[0].shape[1] == d]
+            got = fps.bucket_fps_kdline_sampling_batch([c[0] for c in sub], [c[1] for c in sub],
+                                                        [c[2] for c in sub], [c[3] for c in sub])
+            for (p, k, h, s), g in zip(sub, got):
+                np.testing.assert_array_equal(g, ORACLE.kdline(p, k, h, s, mode))
+    else:
+        for p, k, _, s in cases:
+            np.testing.assert_array_equal(fps.fps_sampling(p, k, s), ORACLE.fps(p, k, [s], mode))
+
+
 def test_batch_with_clouds_too_big_for_shared_memory(mode):
     # one cloud with more piece records than fit in shared memory takes the
     # multi-CTA path inside the same batched call
