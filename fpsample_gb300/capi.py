@@ -46,6 +46,7 @@ SIGNATURES = {
     "fpsgpu_stats_timing": (None, [ctypes.c_int]),
     "fpsgpu_last_error": (ctypes.c_char_p, []),
     "fpsgpu_selftest_exchange_timeout": (ctypes.c_int, []),
+    "fpsgpu_selftest_lead_timeout": (ctypes.c_int, []),
     "fpsgpu_debug_fail_allocations": (None, [ctypes.c_longlong]),
     "fpsgpu_sample_points": (ctypes.c_int, [ctypes.c_int, _f32p, _sz, _sz, _sz, _szp, _sz, _sz,
                                             _szp, _f32p]),

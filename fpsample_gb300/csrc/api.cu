@@ -1011,6 +1011,43 @@ int fpsgpu_selftest_exchange_timeout(void) {
     return check_device_error(err, ctx.stream);
 }
 
+int fpsgpu_selftest_lead_timeout(void) {
+    clear_error();
+    DevCtx ctx;
+    int rc;
+    if ((rc = current_ctx(&ctx))) return rc;
+    // one 20,000-point cloud: more pieces than the hot table, so that the
+    // workers keep some and wait for the (muted) leader
+    const size_t n = 20000, dim = 3;
+    std::vector<float> pts(n * dim);
+    uint32_t x = 12345u;
+    for (float& v : pts) {
+        x = x * 1664525u + 1013904223u;
+        v = (float)(x >> 8) * (1.0f / 16777216.0f);
+    }
+    Scratch sc(ctx.stream);
+    float* d_pts;
+    uint64_t* d_out;
+    if ((rc = sc.alloc(&d_pts, n * dim))) return rc;
+    if ((rc = sc.alloc(&d_out, n / 4))) return rc;
+    FPSGPU_CUDA_TRY(cudaMemcpyAsync(d_pts, pts.data(), n * dim * sizeof(float), cudaMemcpyHostToDevice,
+                                    ctx.stream));
+    BatchCall b;
+    b.d_points = d_pts;
+    b.off = {0, n};
+    b.k = {n / 4};
+    b.start = {0};
+    b.height = {5};
+    b.kd = true;
+    b.d_out = d_out;
+    b.stream = ctx.stream;
+    b.sms = ctx.sms;
+    b.lead_selftest = true;
+    rc = fp_mode() == FPSGPU_FP_FMA ? run_batch_fma((int)dim, b) : run_batch_nofma((int)dim, b);
+    FPSGPU_CUDA_TRY(cudaStreamSynchronize(ctx.stream));
+    return rc;
+}
+
 void fpsgpu_debug_fail_allocations(long long after) { g_alloc_budget.store(after < 0 ? -1 : after); }
 
 int fpsgpu_kdline_build(const float* raw_data, size_t n_points, size_t dim, size_t height,

@@ -2099,6 +2099,9 @@ struct BatchCall {
     // GPU at once with that size; 1: just as many CTAs as the pieces need,
     // which leaves more SMs to other work, e.g. in the server)
     int min_cluster = 0;
+    // self-test of lead_sample's bounded wait (fpsgpu_selftest_lead_timeout):
+    // the leader publishes nothing, the workers give up after 4096 polls
+    bool lead_selftest = false;
 };
 
 // The one-CTA clouds of a batched call (D <= 3) on lead_sample: float4 point
@@ -2160,6 +2163,8 @@ int launch_lead_sampler(const BatchCall& bc, const Built& bt, const std::vector<
     la.counters = cnt;
     la.err = bt.err;
     la.out_pts = bc.d_out_pts;
+    la.spin_limit = bc.lead_selftest ? 4096 : kSpinLimit;
+    la.mute = bc.lead_selftest ? 1 : 0;
     const size_t smem = kLeadSmemBytes;
     if (int arc = allow_max_smem(kern)) return arc;
     int per_sm = 0;
@@ -2215,6 +2220,8 @@ int run_batch(const BatchCall& bc) {
     // one-CTA clouds of D <= 3 take the leader/worker sampler (lead_sample)
     const bool use_lead = D <= 3 && lead_sampler_enabled();
     const uint32_t one_cap = use_lead ? kLeadCap : cap_max;
+    if (bc.lead_selftest && !use_lead)
+        return set_error(FPSGPU_ERR_ARG, "the leader/worker sampler is off (FPSGPU_ONECTA_SAMPLER)");
     const int want_cluster = bc.min_cluster > 0 ? bc.min_cluster : cluster_size_for_batch();
     const uint32_t promote = cluster_min_pieces();
     std::vector<uint64_t> out_off(C), tag0(C);

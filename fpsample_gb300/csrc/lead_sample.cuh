@@ -91,6 +91,8 @@ struct LeadArgs {
     unsigned long long* counters;
     int* err;
     float* out_pts;
+    long long spin_limit;  // polls a worker makes for the next reference before giving up
+    int mute;              // self-test of that bound: the leader publishes nothing
 };
 
 // shared region: the hot pieces' records and leader low key words
@@ -514,7 +516,7 @@ __device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, fl
                 for (;;) {
                     v = ld_acquire_cta_shared(&S.nref);
                     if ((v & ~kLeadDone) > s || (v & kLeadDone)) break;
-                    if (++spins > kSpinLimit) {
+                    if (++spins > a.spin_limit) {
                         gave_up = true;
                         break;
                     }
@@ -572,7 +574,7 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
         bool mod0 = false, mod1 = false;
         uint32_t s = 0;
         uint64_t wk = warp_max_key(k0 > k1 ? k0 : k1);  // the best hot key (warp-uniform)
-        while (emitted < cc.K && s < (uint32_t)kLeadRefs) {
+        while (!a.mute && emitted < cc.K && s < (uint32_t)kLeadRefs) {
             if (wk <= Tb) break;
             const uint32_t e = (uint32_t)wk & 63u, rec = ((uint32_t)wk >> 6) & 127u;
             float4* const ep = s_pt + e * kPiece;
@@ -680,8 +682,8 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
         if (mod0) S.hmod[lane] = 1;
         if (lane == 0) {
             S.emitted = emitted;
-            if (s == 0) S.stall = 1;  // cannot happen: the best piece is always hot
-            st_release_cta_shared(&S.nref, s | kLeadDone);
+            if (s == 0) S.stall = 1;  // cannot happen (but in the self-test): the best piece is always hot
+            if (!a.mute) st_release_cta_shared(&S.nref, s | kLeadDone);
         }
         lead_bar();  // the workers have applied the epoch
         if (S.stall) break;

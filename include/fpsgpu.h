@@ -253,11 +253,18 @@ const char *fpsgpu_last_error(void);
  *     CTA for a grid of two, so the partner never arrives, with a limit of 4096
  *     polls; returns FPSGPU_ERR_DEVICE when the bounded wait works.  The GPU
  *     stays usable afterwards.
+ *   fpsgpu_selftest_lead_timeout: runs the one-CTA leader/worker sampler on a
+ *     20,000-point cloud with the leader muted, so its worker warps wait for
+ *     a sample that never comes, with a limit of 4096 polls; returns
+ *     FPSGPU_ERR_DEVICE when that bounded wait works (FPSGPU_ERR_ARG when
+ *     FPSGPU_ONECTA_SAMPLER=lockstep turned the sampler off).  The GPU stays
+ *     usable afterwards.
  *   fpsgpu_debug_fail_allocations: host-side fault injection.  After `after`
  *     more successful scratch allocations (any thread) every scratch
  *     allocation fails with FPSGPU_ERR_CUDA, until called with -1.
  */
 int fpsgpu_selftest_exchange_timeout(void);
+int fpsgpu_selftest_lead_timeout(void);
 void fpsgpu_debug_fail_allocations(long long after);
 
 /* library version string */

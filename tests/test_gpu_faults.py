@@ -5,6 +5,10 @@
   partner that never arrives (one CTA launched for a grid of two, a limit of
   4096 polls).  The call must return FPSGPU_ERR_DEVICE, and the GPU must stay
   usable: a normal call right after it is still bit-exact.
+* The one-CTA leader/worker sampler's worker warps wait for the leader's next
+  sample with a bounded poll count; fpsgpu_selftest_lead_timeout runs it with
+  the leader muted (a limit of 4096 polls) and must return FPSGPU_ERR_DEVICE,
+  the next call still exact.
 * Host-side fault injection: fpsgpu_debug_fail_allocations refuses the N-th
   scratch allocation.  For every N up to the first one the call survives, the
   call must raise the reference's RuntimeError, and the next call must succeed
@@ -30,6 +34,22 @@ def test_bounded_exchange_wait_reports_an_error_and_the_gpu_stays_usable():
     pts = np.random.default_rng(71).random((3000, 3)).astype(np.float32)
     got = fps.bucket_fps_kdline_sampling(pts, 300, 5, 0)
     np.testing.assert_array_equal(got, Oracle().kdline(pts, 300, 5, 0, fps.get_fp_mode()))
+
+
+def test_bounded_worker_wait_of_the_one_cta_sampler_reports_an_error():
+    """The leader/worker sampler's worker warps wait for the leader's next
+    sample with a bounded poll count; with the leader muted they must give
+    up, the call must return FPSGPU_ERR_DEVICE, and the next call must still
+    be exact."""
+    lib = capi.lib()
+    assert lib.fpsgpu_selftest_lead_timeout() == FPSGPU_ERR_DEVICE
+    assert "gave up" in lib.fpsgpu_last_error().decode()
+    rng = np.random.default_rng(73)
+    clouds = [rng.random((n, 3)).astype(np.float32) for n in (20000, 3000)]
+    got = fps.bucket_fps_kdline_sampling_batch(clouds, [5000, 700], 5, 0)
+    oracle = Oracle()
+    for p, k, g in zip(clouds, (5000, 700), got):
+        np.testing.assert_array_equal(g, oracle.kdline(p, k, 5, 0, fps.get_fp_mode()))
 
 
 @pytest.mark.parametrize("algo", ["kdline", "vanilla", "batch"])

@@ -380,6 +380,38 @@ def test_one_cta_sampler_epochs_with_ties(kind, mode):
             np.testing.assert_array_equal(fps.fps_sampling(p, k, s), ORACLE.fps(p, k, [s], mode))
 
 
+_LOCKSTEP_CHILD = r"""
+import sys
+import numpy as np
+import fpsample as fps
+data = np.load(sys.argv[1], allow_pickle=True)
+fps.set_fp_mode(str(data["mode"]))
+got = fps.bucket_fps_kdline_sampling_batch(list(data["clouds"]), list(data["ks"]), list(data["hs"]),
+                                           list(data["ss"]))
+np.save(sys.argv[2], np.array(got, dtype=object), allow_pickle=True)
+"""
+
+
+def test_lockstep_one_cta_sampler_d3(mode, tmp_path):
+    """The lockstep one-CTA sampler (batch_sample), which D <= 3 clouds take
+    only with FPSGPU_ONECTA_SAMPLER=lockstep (read once per process, hence a
+    child process), against the oracle."""
+    import os
+    import subprocess
+    import sys
+
+    clouds, ks, hs, ss = _batch_clouds(31, 12, 500, 60000, 3)
+    inp, out = tmp_path / "in.npz", tmp_path / "out.npy"
+    np.savez(inp, clouds=np.array(clouds, dtype=object), ks=ks, hs=hs, ss=ss, mode=mode)
+    env = dict(os.environ, FPSGPU_ONECTA_SAMPLER="lockstep")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.run([sys.executable, "-c", _LOCKSTEP_CHILD, str(inp), str(out)], env=env, cwd=root,
+                   check=True, timeout=600)
+    got = np.load(out, allow_pickle=True)
+    for p, k, h, s, g in zip(clouds, ks, hs, ss, got):
+        np.testing.assert_array_equal(g, ORACLE.kdline(p, k, h, s, mode))
+
+
 def test_batch_with_clouds_too_big_for_shared_memory(mode):
     # one cloud with more piece records than fit in shared memory takes the
     # multi-CTA path inside the same batched call
