@@ -27,8 +27,8 @@
 // to T (or the reference list is full) the epoch ends at a CTA barrier.  No
 // sample waits for the workers.
 //
-// Leader keys.  A hot record's low key word is (position << 13) | (record
-// << 6) | entry, with the cloud-local position in 18 bits (complemented for
+// Leader keys.  A hot record's low key word is (position << 14) | (record
+// << 7) | entry, with the cloud-local position in 18 bits (complemented for
 // kd-line, like batch_key): the order is the reference's tie order (position
 // first, and positions are unique), and the warp max itself names the winner's
 // entry and record, so the next reference point is one shared load away.  Hot
@@ -52,23 +52,23 @@ constexpr int kLeadThreads = 384;
 constexpr int kLeadWorkers = kLeadThreads / 32 - 1;  // warps 1..11
 constexpr int kLeadSlots = 5;                        // pieces per worker thread (<= 8: hent)
 constexpr uint32_t kLeadCap = (uint32_t)kLeadWorkers * 32 * kLeadSlots;  // 1760 pieces
-constexpr int kLeadHotPerWarp = 5;
-constexpr int kLeadHot = kLeadWorkers * kLeadHotPerWarp;  // 55 hot pieces
+constexpr int kLeadHotPerWarp = 7;
+constexpr int kLeadHot = kLeadWorkers * kLeadHotPerWarp;  // 77 hot pieces
 constexpr int kLeadRefs = 128;                            // samples per epoch at most
 constexpr uint32_t kLeadDone = 0x80000000u;               // epoch-end bit of the reference count
 constexpr uint32_t kLeadHotPoints = (uint32_t)kLeadHot * kPiece;
-// leader key low word: position (18 bits) | record (7 bits) | entry (6 bits)
+// leader key low word: position (18 bits) | record (7 bits) | entry (7 bits)
 constexpr uint32_t kLeadPosBits = 18;
 constexpr uint32_t kLeadPosMask = (1u << kLeadPosBits) - 1;
 // clouds the leader sampler takes: positions fit its keys
 constexpr uint64_t kLeadMaxCloudPoints = 1ull << kLeadPosBits;
 
-static_assert(kLeadHot <= 64, "entries fit 6 bits; the leader holds two per lane");
+static_assert(kLeadHot <= 96, "entries fit 7 bits; the leader holds three per lane");
 static_assert(kPiece == 128, "records of a piece fit 7 bits, four per lane");
 static_assert(kLeadCap <= (1u << kBatchPieceBits), "piece index must fit batch_key");
-static_assert(kLeadPosBits + 7 + 6 <= 32, "leader key low word");
+static_assert(kLeadPosBits + 7 + 7 <= 32, "leader key low word");
 static_assert((uint64_t)kLeadCap * kPiece <= kLeadMaxCloudPoints, "positions of a one-CTA cloud fit 18 bits");
-static_assert(kLeadPosBits + 8 + 6 <= 32, "fill word: entry | piece start | length");
+static_assert(kLeadPosBits + 8 <= 32, "fill word: piece start | length");
 
 struct LeadArgs {
     float4* P4;             // [n] {x, y, z, running distance}, storage order
@@ -161,17 +161,33 @@ __device__ __forceinline__ uint32_t lead_loc_worker(uint32_t lo) {
 }
 template <bool KD>
 __device__ __forceinline__ uint32_t lead_loc_leader(uint32_t lo) {
-    const uint32_t f = (lo >> 13) & kLeadPosMask;
+    const uint32_t f = (lo >> 14) & kLeadPosMask;
     return KD ? kLeadPosMask - f : f;
 }
 template <bool KD>
 __device__ __forceinline__ uint32_t lead_pos_leader(uint32_t loc) {
-    return (KD ? kLeadPosMask - loc : loc) << 13;
+    return (KD ? kLeadPosMask - loc : loc) << 14;
 }
 template <bool KD>
 __device__ __forceinline__ uint32_t lead_pos_worker(uint32_t loc) {
     const uint32_t pm = (1u << kBatchPosBits) - 1;
     return (KD ? pm - loc : loc) << kBatchPieceBits;
+}
+
+// box_bound on float4 boxes and reference (the same operations, D <= 3)
+template <int D, bool FMA>
+__device__ __forceinline__ float lead_box_bound4(const float4& lo, const float4& hi, const float4& r) {
+    float g = fmaxf(fmaxf(__fsub_rn(lo.x, r.x), __fsub_rn(r.x, hi.x)), 0.0f);
+    float acc = __fmul_rn(g, g);
+    if (D > 1) {
+        g = fmaxf(fmaxf(__fsub_rn(lo.y, r.y), __fsub_rn(r.y, hi.y)), 0.0f);
+        acc = FMA ? __fmaf_rn(g, g, acc) : __fadd_rn(acc, __fmul_rn(g, g));
+    }
+    if (D > 2) {
+        g = fmaxf(fmaxf(__fsub_rn(lo.z, r.z), __fsub_rn(r.z, hi.z)), 0.0f);
+        acc = FMA ? __fmaf_rn(g, g, acc) : __fadd_rn(acc, __fmul_rn(g, g));
+    }
+    return acc;
 }
 
 // max of (h, l) pairs, h first
@@ -261,18 +277,19 @@ __device__ __forceinline__ void lead_bar() {
 
 // Shared state of one CTA (besides the dynamic region of hot records).
 struct LeadShared {
-    uint64_t hkey[64];         // hot table: key (leader format; 0: empty entry)
-    float4 hlo[64], hhi[64];   // box
-    uint32_t hlen[64];         // records of the piece
-    uint32_t hps[64];          // piece start (cloud-local)
-    uint8_t hmod[64];          // the leader lowered a distance since the entry was filled
+    uint64_t hkey[96];         // hot table: key (leader format; 0: empty entry)
+    float4 hlo[96], hhi[96];   // box
+    uint32_t hlen[96];         // records of the piece
+    uint32_t hps[96];          // piece start (cloud-local)
+    uint8_t hmod[96];          // the leader lowered a distance since the entry was filled
     float4 ref[kLeadRefs];     // this epoch's references, in order (their coordinates are the outputs' points)
     uint32_t outq[kLeadRefs];  // this epoch's outputs (cloud-local position), written out after the epoch
     uint32_t nref;             // references published | kLeadDone at the epoch's end
     uint64_t T[kLeadWorkers];  // best non-hot key of every worker warp (worker format)
     uint32_t wlo[kLeadWorkers][kLeadSlots][32];  // workers: low word of every slot's key
     uint32_t wpr[kLeadWorkers][kLeadSlots][32];  // workers: piece start (cloud-local) << 8 | length
-    uint32_t fill[kLeadWorkers][kLeadHotPerWarp];  // workers: entries to copy in: entry << 26 | piece start << 8 | length
+    uint32_t fill[kLeadWorkers][kLeadHotPerWarp];  // workers: pieces to copy in: piece start << 8 | length
+    uint8_t fent[kLeadWorkers][kLeadHotPerWarp];   // and their entries
     uint64_t fkey[kLeadWorkers][kLeadHotPerWarp];  // and their keys (worker format)
     uint32_t item;
     uint32_t emitted;
@@ -450,7 +467,8 @@ __device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, fl
                     }
                     S.hlo[e] = l4;
                     S.hhi[e] = h4;
-                    S.fill[w][nfill] = (e << 26) | wpr[j][l];
+                    S.fill[w][nfill] = wpr[j][l];
+                    S.fent[w][nfill] = (uint8_t)e;
                     S.fkey[w][nfill] = full_key(j);
                     S.hkey[e] = 0ull;  // set by the copy below
                 }
@@ -470,7 +488,7 @@ __device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, fl
         for (uint32_t fi = 0; fi < nfill; ++fi) {
             const uint32_t f = S.fill[w][fi];
             const uint64_t fkey = S.fkey[w][fi];
-            const uint32_t e = f >> 26, ps = (f >> 8) & kLeadPosMask, len = f & 0xffu;
+            const uint32_t e = S.fent[w][fi], ps = f >> 8, len = f & 0xffu;
             float4 x[kPiece / 32];
             uint32_t lw[kPiece / 32];
 #pragma unroll
@@ -482,7 +500,7 @@ __device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, fl
 #pragma unroll
             for (int j = 0; j < kPiece / 32; ++j) {
                 const uint32_t i = lane + 32 * j, ri = i < len ? i : len - 1;
-                const uint32_t ll = lead_pos_leader<KD>(lead_loc_worker<KD>(lw[j])) | (ri << 6) | e;
+                const uint32_t ll = lead_pos_leader<KD>(lead_loc_worker<KD>(lw[j])) | (ri << 7) | e;
                 s_pt[e * kPiece + i] = x[j];
                 s_lw[e * kPiece + i] = ll;
                 const uint64_t kk = ((uint64_t)(__float_as_uint(x[j].w) | 0x80000000u) << 32) | lw[j];
@@ -552,9 +570,10 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
                                             const LeadCloud& cc, unsigned long long& tested,
                                             unsigned long long& touched) {
     const uint32_t lane = threadIdx.x & 31;
-    const bool has1 = lane + 32 < (uint32_t)kLeadHot;
+    const bool has1 = lane + 32 < (uint32_t)kLeadHot, has2 = lane + 64 < (uint32_t)kLeadHot;
     S.hkey[lane] = 0ull;  // every entry starts empty
     S.hkey[lane + 32] = 0ull;
+    S.hkey[lane + 64] = 0ull;
     if (lane == 0) S.stall = 0;
     lead_bar();  // the workers' first reference
 
@@ -564,19 +583,23 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
         lead_bar();                 // the hot table is ready
         // T in leader format: the position decides ties, the rest is all ones
         uint64_t Tb = warp_max_key(lane < (uint32_t)kLeadWorkers ? S.T[lane] : 0ull);
-        if (Tb) Tb = (Tb & 0xffffffff00000000ull) | lead_pos_leader<KD>(lead_loc_worker<KD>((uint32_t)Tb)) | 0x1fffu;
-        uint64_t k0 = S.hkey[lane], k1 = has1 ? S.hkey[lane + 32] : 0ull;
+        if (Tb) Tb = (Tb & 0xffffffff00000000ull) | lead_pos_leader<KD>(lead_loc_worker<KD>((uint32_t)Tb)) | 0x3fffu;
+        uint64_t k0 = S.hkey[lane], k1 = has1 ? S.hkey[lane + 32] : 0ull, k2 = has2 ? S.hkey[lane + 64] : 0ull;
         const float4 l0 = S.hlo[lane], h0 = S.hhi[lane];
         const float4 l1 = has1 ? S.hlo[lane + 32] : make_float4(INFINITY, INFINITY, INFINITY, 0.0f);
         const float4 h1 = has1 ? S.hhi[lane + 32] : make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
-        const float lo0[3] = {l0.x, l0.y, l0.z}, hi0[3] = {h0.x, h0.y, h0.z};
-        const float lo1[3] = {l1.x, l1.y, l1.z}, hi1[3] = {h1.x, h1.y, h1.z};
-        bool mod0 = false, mod1 = false;
+        const float4 l2 = has2 ? S.hlo[lane + 64] : make_float4(INFINITY, INFINITY, INFINITY, 0.0f);
+        const float4 h2 = has2 ? S.hhi[lane + 64] : make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
+        bool mod0 = false, mod1 = false, mod2 = false;
         uint32_t s = 0;
-        uint64_t wk = warp_max_key(k0 > k1 ? k0 : k1);  // the best hot key (warp-uniform)
+        auto max3 = [](uint64_t x, uint64_t y, uint64_t z) {
+            const uint64_t m = x > y ? x : y;
+            return m > z ? m : z;
+        };
+        uint64_t wk = warp_max_key(max3(k0, k1, k2));  // the best hot key (warp-uniform)
         while (!a.mute && emitted < cc.K && s < (uint32_t)kLeadRefs) {
             if (wk <= Tb) break;
-            const uint32_t e = (uint32_t)wk & 63u, rec = ((uint32_t)wk >> 6) & 127u;
+            const uint32_t e = (uint32_t)wk & 127u, rec = ((uint32_t)wk >> 7) & 127u;
             float4* const ep = s_pt + e * kPiece;
             const uint32_t* const el = s_lw + e * kPiece;
             const float4 r = ep[rec];
@@ -599,11 +622,11 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
             ++s;
             // the other entries' box tests do not depend on the winner's
             // recompute (branch-free, so they share its basic block)
-            const bool o0 = lane != e, o1 = lane + 32 != e;
-            const uint64_t x0 = o0 ? k0 : 0ull, x1 = o1 ? k1 : 0ull;
-            const float rv[3] = {r.x, r.y, r.z};
-            const bool d0 = (x0 != 0) & (box_bound<D, FMA>(lo0, hi0, rv) < key_dist(x0));
-            const bool d1 = (x1 != 0) & (box_bound<D, FMA>(lo1, hi1, rv) < key_dist(x1));
+            const bool o0 = lane != e, o1 = lane + 32 != e, o2 = lane + 64 != e;
+            const uint64_t x0 = o0 ? k0 : 0ull, x1 = o1 ? k1 : 0ull, x2 = o2 ? k2 : 0ull;
+            const bool d0 = (x0 != 0) & (lead_box_bound4<D, FMA>(l0, h0, r) < key_dist(x0));
+            const bool d1 = (x1 != 0) & (lead_box_bound4<D, FMA>(l1, h1, r) < key_dist(x1));
+            const bool d2 = (x2 != 0) & (lead_box_bound4<D, FMA>(l2, h2, r) < key_dist(x2));
             // the winner's recompute
             uint32_t bh[kPiece / 32];
 #pragma unroll
@@ -623,6 +646,7 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
             // reductions issue side by side.
             uint32_t ch = (uint32_t)(x0 >> 32), cl = (uint32_t)x0;
             lead_pmax(ch, cl, (uint32_t)(x1 >> 32), (uint32_t)x1);
+            lead_pmax(ch, cl, (uint32_t)(x2 >> 32), (uint32_t)x2);
             lead_pmax(ch, cl, bh[0], w[0]);
             const uint32_t ah = __reduce_max_sync(kFull, ch);
             const uint32_t nh = __reduce_max_sync(kFull, bh[0]);
@@ -631,9 +655,11 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
             const uint64_t nk = ((uint64_t)nh << 32) | nl;
             k0 = o0 ? k0 : nk;
             k1 = o1 ? k1 : nk;
+            k2 = o2 ? k2 : nk;
             mod0 |= !o0;
             mod1 |= !o1;
-            if (__any_sync(kFull, d0 || d1)) {
+            mod2 |= !o2;
+            if (__any_sync(kFull, d0 || d1 || d2)) {
                 // every other hot entry whose box is nearer than its key
                 uint32_t m = __ballot_sync(kFull, d0);
                 while (m) {
@@ -657,7 +683,18 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
                         mod1 = true;
                     }
                 }
-                wk = warp_max_key(k0 > k1 ? k0 : k1);
+                m = __ballot_sync(kFull, d2);
+                while (m) {
+                    const uint32_t l = __ffs(m) - 1;
+                    m &= m - 1;
+                    touched += lane == 0 ? kPiece : 0u;
+                    const uint64_t k = lead_update_hot<D, FMA>(s_pt + (l + 64) * kPiece, s_lw + (l + 64) * kPiece, r);
+                    if (lane == l) {
+                        k2 = k;
+                        mod2 = true;
+                    }
+                }
+                wk = warp_max_key(max3(k0, k1, k2));
             } else {
                 wk = ((uint64_t)ah << 32) | al;  // nothing else changed
             }
@@ -678,6 +715,10 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
         if (has1) {
             S.hkey[lane + 32] = k1;
             if (mod1) S.hmod[lane + 32] = 1;
+        }
+        if (has2) {
+            S.hkey[lane + 64] = k2;
+            if (mod2) S.hmod[lane + 64] = 1;
         }
         if (mod0) S.hmod[lane] = 1;
         if (lane == 0) {
