@@ -175,6 +175,16 @@ bool lead_sampler_enabled() {
     return v;
 }
 
+int lead_hot_per_warp() {
+    static const int v = [] {
+        const char* e = std::getenv("FPSGPU_LEAD_HOT");
+        if (!e) return 0;
+        const int x = std::atoi(e);
+        return x == 5 || x == 7 ? x : 0;
+    }();
+    return v;
+}
+
 int cluster_size_for_batch() {
     static const int v = [] {
         const char* e = std::getenv("FPSGPU_CLUSTER_SIZE");

@@ -2113,7 +2113,7 @@ int launch_lead_sampler(const BatchCall& bc, const Built& bt, const std::vector<
                         const std::vector<uint32_t>& clustered, const uint32_t* d_order, unsigned int* d_queue,
                         const uint64_t* d_coff, const uint32_t* d_cpiece, const uint64_t* d_k,
                         const uint64_t* d_tag0, const uint64_t* d_ooff, unsigned long long* cnt, bool both,
-                        int cl, int maxc, int smem_optin, Scratch& sc) {
+                        int cl, int maxc, int smem_optin, uint32_t max_pieces, Scratch& sc) {
     const size_t C = bc.off.size() - 1;
     const uint64_t n = bc.off[C];
     int rc;
@@ -2132,16 +2132,29 @@ int launch_lead_sampler(const BatchCall& bc, const Built& bt, const std::vector<
                                                                  (uint32_t)C, P4, LW);
         FPSGPU_CUDA_TRY(cudaGetLastError());
     }
-    const void* kern = bc.kd ? (const void*)lead_sample<D, FMA, true> : (const void*)lead_sample<D, FMA, false>;
+    // the 77-entry table when the launch holds a cloud of kLeadHotWideMin
+    // pieces or more (D = 3 only; FPSGPU_LEAD_HOT=5|7 forces one)
+    const int hpw_forced = lead_hot_per_warp();
+    const bool wide = D == 3 && (hpw_forced ? hpw_forced == kLeadHotPerWarp : max_pieces >= kLeadHotWideMin);
+    const void* kern = nullptr;
+    if constexpr (D == 3) {
+        if (wide)
+            kern = bc.kd ? (const void*)lead_sample<D, FMA, true, kLeadHotPerWarp>
+                         : (const void*)lead_sample<D, FMA, false, kLeadHotPerWarp>;
+    }
+    if (!kern)
+        kern = bc.kd ? (const void*)lead_sample<D, FMA, true, kLeadHotSmall>
+                     : (const void*)lead_sample<D, FMA, false, kLeadHotSmall>;
     size_t static_smem = 0;
     {
         cudaFuncAttributes fa{};
         FPSGPU_CUDA_TRY(cudaFuncGetAttributes(&fa, kern));
         static_smem = fa.sharedSizeBytes;
     }
-    if (static_smem + kLeadSmemBytes + 256 > (size_t)smem_optin)
+    const size_t smem = lead_smem_bytes((uint32_t)kLeadWorkers * (wide ? kLeadHotPerWarp : kLeadHotSmall));
+    if (static_smem + smem + 256 > (size_t)smem_optin)
         return set_error(FPSGPU_ERR_CUDA, "lead_sample needs %zu bytes of shared memory, the device offers %d",
-                         static_smem + kLeadSmemBytes, smem_optin);
+                         static_smem + smem, smem_optin);
     LeadArgs la{};
     la.P4 = P4;
     la.LW = LW;
@@ -2165,7 +2178,6 @@ int launch_lead_sampler(const BatchCall& bc, const Built& bt, const std::vector<
     la.out_pts = bc.d_out_pts;
     la.spin_limit = bc.lead_selftest ? 4096 : kSpinLimit;
     la.mute = bc.lead_selftest ? 1 : 0;
-    const size_t smem = kLeadSmemBytes;
     if (int arc = allow_max_smem(kern)) return arc;
     int per_sm = 0;
     FPSGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kLeadThreads, smem));
@@ -2350,7 +2362,7 @@ int run_batch(const BatchCall& bc) {
             if constexpr (D <= 3) {
                 if ((rc = launch_lead_sampler<D, FMA>(bc, bt, small, clustered, d_order, d_queue, d_coff,
                                                       d_cpiece, d_k, d_tag0, d_ooff, cnt, both, cl, maxc,
-                                                      smem_optin, sc)))
+                                                      smem_optin, cap, sc)))
                     return rc;
             }
         } else if (!small.empty()) {

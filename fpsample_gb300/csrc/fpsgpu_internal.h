@@ -174,6 +174,9 @@ int cluster_size_for_batch();
 // One-CTA batched clouds of D <= 3 take the leader/worker sampler unless
 // FPSGPU_ONECTA_SAMPLER=lockstep selects the lockstep one (batch_sample).
 bool lead_sampler_enabled();
+// Hot pieces per worker warp of the leader/worker sampler: FPSGPU_LEAD_HOT
+// (5 or 7) fixes the table for every launch; 0 (unset): the size rule.
+int lead_hot_per_warp();
 bool cluster_size_fixed();
 uint32_t cluster_min_pieces();
 int cluster_capacity(const void* func, int cl, int block, size_t smem, int* out);

@@ -11,29 +11,29 @@
 // whose old key beats the best key of the pieces that r_t left alone -- in
 // practice the winner's own piece and the runner-up.
 //
-// Design.  Warp 0 (the leader) holds a hot table of up to kLeadHot pieces in
-// shared memory: at the start of an epoch every worker warp names its
-// kLeadHotPerWarp pieces of largest key; pieces that were hot already stay
-// where they are, new ones are copied in, pieces that drop out are written
-// back.  T = the largest key of the pieces left with the workers at that
-// moment.  Keys only fall, so T bounds every non-hot piece for the whole
-// epoch, and while the best hot key exceeds T the best hot piece holds the
-// global argmax.  The leader then runs alone: take the best hot key, emit its
-// point (into a shared output queue and the epoch's reference list), recompute
-// its piece at once (the winner's piece is always dirty), then every other hot
-// piece whose box is nearer than its key, repeat.  Workers (warps 1..11) apply
-// the same references, in order and asynchronously, to the pieces they kept
-// (box tests and recomputes as in batch_sample).  When the best hot key falls
-// to T (or the reference list is full) the epoch ends at a CTA barrier.  No
-// sample waits for the workers.
+// Design.  Warp 0 (the leader) holds a hot table of 55 or 77 pieces in
+// shared memory: at the start of an epoch every worker warp names its 5 or 7
+// pieces of largest key; pieces that were hot already stay where they are,
+// new ones are copied in, pieces that drop out are written back.  T = the
+// largest key of the pieces left with the workers at that moment.  Keys only
+// fall, so T bounds every non-hot piece for the whole epoch, and while the
+// best hot key exceeds T the best hot piece holds the global argmax.  The
+// leader then runs alone: take the best hot key, emit its point (into a
+// shared output queue and the epoch's reference list), recompute its piece at
+// once (the winner's piece is always dirty), then every other hot piece whose
+// box is nearer than its key, repeat.  Workers (warps 1..11) apply the same
+// references, in order and asynchronously, to the pieces they kept (box tests
+// and recomputes as in batch_sample).  When the best hot key falls to T (or
+// the reference list is full) the epoch ends at a CTA barrier.  No sample
+// waits for the workers.
 //
-// Leader keys.  A hot record's low key word is (position << 14) | (record
-// << 7) | entry, with the cloud-local position in 18 bits (complemented for
-// kd-line, like batch_key): the order is the reference's tie order (position
-// first, and positions are unique), and the warp max itself names the winner's
-// entry and record, so the next reference point is one shared load away.  Hot
-// entries are padded to kPiece records with copies of their last record (same
-// key), so a recompute needs no bounds.
+// Leader keys.  A hot record's low key word is position | record (7 bits) |
+// entry (6 bits, 7 for the 77-entry table), with the cloud-local position in
+// 18 bits (complemented for kd-line, like batch_key): the order is the
+// reference's tie order (position first, and positions are unique), and the
+// warp max itself names the winner's entry and record, so the next reference
+// point is one shared load away.  Hot entries are padded to kPiece records
+// with copies of their last record (same key), so a recompute needs no bounds.
 //
 // Exactness.  Hot pieces are kept exact (every sample applied, in order); a
 // non-hot piece's stored key only ever over-states its true key, and the
@@ -52,12 +52,26 @@ constexpr int kLeadThreads = 384;
 constexpr int kLeadWorkers = kLeadThreads / 32 - 1;  // warps 1..11
 constexpr int kLeadSlots = 5;                        // pieces per worker thread (<= 8: hent)
 constexpr uint32_t kLeadCap = (uint32_t)kLeadWorkers * 32 * kLeadSlots;  // 1760 pieces
-constexpr int kLeadHotPerWarp = 7;
-constexpr int kLeadHot = kLeadWorkers * kLeadHotPerWarp;  // 77 hot pieces
+// Hot pieces per worker warp (HPW, a template parameter): 5 (a table of 55
+// entries, two per leader lane) or 7 (77 entries, three per lane).  Longer
+// epochs pay on large clouds; on clouds of fewer than kLeadHotWideMin pieces
+// the narrow table is faster (the workers keep a larger share of the dirty
+// pieces), so a launch takes the wide one when its largest cloud has that many.
+constexpr int kLeadHotPerWarp = 7;                        // the wide table
+constexpr int kLeadHot = kLeadWorkers * kLeadHotPerWarp;  // 77 entries at most
+constexpr int kLeadHotSmall = 5;                          // the narrow table (55 entries)
+constexpr uint32_t kLeadHotWideMin = 512;
+// the layout of a table of HPW hot pieces per worker warp
+template <int HPW>
+struct LeadTable {
+    static constexpr int kHot = kLeadWorkers * HPW;
+    // leader key low word: position (18 bits) | record (7 bits) | entry (kEntryBits)
+    static constexpr uint32_t kEntryBits = kHot <= 64 ? 6 : 7;
+    static constexpr uint32_t kPosShift = kEntryBits + 7;
+    static constexpr bool kThree = kHot > 64;  // three entries per leader lane
+};
 constexpr int kLeadRefs = 128;                            // samples per epoch at most
 constexpr uint32_t kLeadDone = 0x80000000u;               // epoch-end bit of the reference count
-constexpr uint32_t kLeadHotPoints = (uint32_t)kLeadHot * kPiece;
-// leader key low word: position (18 bits) | record (7 bits) | entry (7 bits)
 constexpr uint32_t kLeadPosBits = 18;
 constexpr uint32_t kLeadPosMask = (1u << kLeadPosBits) - 1;
 // clouds the leader sampler takes: positions fit its keys
@@ -68,7 +82,7 @@ static_assert(kPiece == 128, "records of a piece fit 7 bits, four per lane");
 static_assert(kLeadCap <= (1u << kBatchPieceBits), "piece index must fit batch_key");
 static_assert(kLeadPosBits + 7 + 7 <= 32, "leader key low word");
 static_assert((uint64_t)kLeadCap * kPiece <= kLeadMaxCloudPoints, "positions of a one-CTA cloud fit 18 bits");
-static_assert(kLeadPosBits + 8 <= 32, "fill word: piece start | length");
+static_assert(kLeadPosBits + 8 + 6 <= 32, "fill word: entry (6-bit entries) | piece start | length");
 
 struct LeadArgs {
     float4* P4;             // [n] {x, y, z, running distance}, storage order
@@ -95,8 +109,9 @@ struct LeadArgs {
     int mute;              // self-test of that bound: the leader publishes nothing
 };
 
-// shared region: the hot pieces' records and leader low key words
-constexpr size_t kLeadSmemBytes = (size_t)kLeadHotPoints * 20;
+// shared region of a table of `entries` hot pieces: their records, then
+// their leader low key words
+constexpr size_t lead_smem_bytes(uint32_t entries) { return (size_t)entries * kPiece * 20; }
 
 // P4 and LW for every point of every piece: coordinates from the SoA X, the
 // low key word batch_key would build from the point's tag and cloud-local
@@ -159,35 +174,19 @@ __device__ __forceinline__ uint32_t lead_loc_worker(uint32_t lo) {
     const uint32_t pm = (1u << kBatchPosBits) - 1, f = (lo >> kBatchPieceBits) & pm;
     return KD ? pm - f : f;
 }
-template <bool KD>
+template <bool KD, int HPW>
 __device__ __forceinline__ uint32_t lead_loc_leader(uint32_t lo) {
-    const uint32_t f = (lo >> 14) & kLeadPosMask;
+    const uint32_t f = (lo >> LeadTable<HPW>::kPosShift) & kLeadPosMask;
     return KD ? kLeadPosMask - f : f;
 }
-template <bool KD>
+template <bool KD, int HPW>
 __device__ __forceinline__ uint32_t lead_pos_leader(uint32_t loc) {
-    return (KD ? kLeadPosMask - loc : loc) << 14;
+    return (KD ? kLeadPosMask - loc : loc) << LeadTable<HPW>::kPosShift;
 }
 template <bool KD>
 __device__ __forceinline__ uint32_t lead_pos_worker(uint32_t loc) {
     const uint32_t pm = (1u << kBatchPosBits) - 1;
     return (KD ? pm - loc : loc) << kBatchPieceBits;
-}
-
-// box_bound on float4 boxes and reference (the same operations, D <= 3)
-template <int D, bool FMA>
-__device__ __forceinline__ float lead_box_bound4(const float4& lo, const float4& hi, const float4& r) {
-    float g = fmaxf(fmaxf(__fsub_rn(lo.x, r.x), __fsub_rn(r.x, hi.x)), 0.0f);
-    float acc = __fmul_rn(g, g);
-    if (D > 1) {
-        g = fmaxf(fmaxf(__fsub_rn(lo.y, r.y), __fsub_rn(r.y, hi.y)), 0.0f);
-        acc = FMA ? __fmaf_rn(g, g, acc) : __fadd_rn(acc, __fmul_rn(g, g));
-    }
-    if (D > 2) {
-        g = fmaxf(fmaxf(__fsub_rn(lo.z, r.z), __fsub_rn(r.z, hi.z)), 0.0f);
-        acc = FMA ? __fmaf_rn(g, g, acc) : __fadd_rn(acc, __fmul_rn(g, g));
-    }
-    return acc;
 }
 
 // max of (h, l) pairs, h first
@@ -275,22 +274,26 @@ __device__ __forceinline__ void lead_bar() {
     asm volatile("barrier.sync 1, %0;" ::"r"(kLeadThreads) : "memory");
 }
 
-// Shared state of one CTA (besides the dynamic region of hot records).
+// Shared state of one CTA (besides the dynamic region of hot records), sized
+// for the table: the narrow kernel's whole shared memory stays within the
+// 164 KB carve-out, which leaves 92 KB of L1 to the workers' pieces.
+template <int HPW>
 struct LeadShared {
-    uint64_t hkey[96];         // hot table: key (leader format; 0: empty entry)
-    float4 hlo[96], hhi[96];   // box
-    uint32_t hlen[96];         // records of the piece
-    uint32_t hps[96];          // piece start (cloud-local)
-    uint8_t hmod[96];          // the leader lowered a distance since the entry was filled
+    static constexpr int kEnt = LeadTable<HPW>::kThree ? 96 : 64;  // 32 per leader lane slot
+    uint64_t hkey[kEnt];         // hot table: key (leader format; 0: empty entry)
+    float4 hlo[kEnt], hhi[kEnt];  // box
+    uint32_t hlen[kEnt];         // records of the piece
+    uint32_t hps[kEnt];          // piece start (cloud-local)
+    uint8_t hmod[kEnt];          // the leader lowered a distance since the entry was filled
     float4 ref[kLeadRefs];     // this epoch's references, in order (their coordinates are the outputs' points)
     uint32_t outq[kLeadRefs];  // this epoch's outputs (cloud-local position), written out after the epoch
     uint32_t nref;             // references published | kLeadDone at the epoch's end
     uint64_t T[kLeadWorkers];  // best non-hot key of every worker warp (worker format)
     uint32_t wlo[kLeadWorkers][kLeadSlots][32];  // workers: low word of every slot's key
     uint32_t wpr[kLeadWorkers][kLeadSlots][32];  // workers: piece start (cloud-local) << 8 | length
-    uint32_t fill[kLeadWorkers][kLeadHotPerWarp];  // workers: pieces to copy in: piece start << 8 | length
-    uint8_t fent[kLeadWorkers][kLeadHotPerWarp];   // and their entries
-    uint64_t fkey[kLeadWorkers][kLeadHotPerWarp];  // and their keys (worker format)
+    uint32_t fill[kLeadWorkers][HPW];  // workers: pieces to copy in: [entry << 26 |] piece start << 8 | length
+    uint8_t fent[kLeadWorkers][LeadTable<HPW>::kEntryBits == 6 ? 1 : HPW];  // and their entries (7-bit entries)
+    uint64_t fkey[kLeadWorkers][HPW];  // and their keys (worker format)
     uint32_t item;
     uint32_t emitted;
     int stall;
@@ -307,8 +310,8 @@ struct LeadCloud {
 // the first reference, then per epoch the hot selection and the epoch's
 // references on the pieces it kept.  Reaches lead_bar() once after the first
 // reference and twice per epoch, like lead_leader.
-template <int D, bool FMA, bool KD>
-__device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, float4* s_pt, uint32_t* s_lw,
+template <int D, bool FMA, bool KD, int HPW>
+__device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared<HPW>& S, float4* s_pt, uint32_t* s_lw,
                                             const LeadCloud& cc, float4 r, int w, unsigned long long& tested,
                                             unsigned long long& touched, bool& gave_up) {
     const uint32_t lane = threadIdx.x & 31;
@@ -317,7 +320,8 @@ __device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, fl
     const uint32_t* const gL = a.LW + cc.coff;
     uint32_t(&wlo)[kLeadSlots][32] = S.wlo[w];  // low word of every slot's key
     uint32_t(&wpr)[kLeadSlots][32] = S.wpr[w];  // cloud-local start << 8 | length
-    const uint32_t e0 = (uint32_t)w * kLeadHotPerWarp;  // my hot entries: e0 .. e0 + 4
+    using Tab = LeadTable<HPW>;
+    const uint32_t e0 = (uint32_t)w * HPW;  // my hot entries: e0 .. e0 + HPW - 1
 
     // slot j of lane l holds cloud piece (j * 32 + l) * kLeadWorkers + w
     // (neighbours in storage order go to different warps)
@@ -386,15 +390,15 @@ __device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, fl
                 const uint64_t k = S.hkey[(uint32_t)(hent >> (8 * j)) & 0xffu];
                 const uint32_t q = ((uint32_t)j * 32 + lane) * kLeadWorkers + (uint32_t)w;
                 kd[j] = key_dist(k);
-                wlo[j][lane] = lead_pos_worker<KD>(lead_loc_leader<KD>((uint32_t)k)) | q;
+                wlo[j][lane] = lead_pos_worker<KD>(lead_loc_leader<KD, HPW>((uint32_t)k)) | q;
             }
         }
-        // ---- the new hot set: my kLeadHotPerWarp pieces of largest key
+        // ---- the new hot set: my HPW pieces of largest key
         uint32_t picked = 0;
         uint64_t fk[kLeadSlots];  // every slot's key, for the picks
 #pragma unroll
         for (int j = 0; j < kLeadSlots; ++j) fk[j] = full_key(j);
-        for (int i = 0; i < kLeadHotPerWarp; ++i) {
+        for (int i = 0; i < HPW; ++i) {
             uint64_t lk = 0;
             int lj = 0;
 #pragma unroll
@@ -431,7 +435,7 @@ __device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, fl
         // new picks take the free entries, lowest first
         uint32_t nfill = 0;
         {
-            uint32_t freem = ~kept & ((1u << kLeadHotPerWarp) - 1);
+            uint32_t freem = ~kept & ((1u << HPW) - 1);
             uint32_t nh = hotm & picked;
             uint64_t ne = 0;
 #pragma unroll
@@ -467,8 +471,12 @@ __device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, fl
                     }
                     S.hlo[e] = l4;
                     S.hhi[e] = h4;
-                    S.fill[w][nfill] = wpr[j][l];
-                    S.fent[w][nfill] = (uint8_t)e;
+                    if constexpr (Tab::kEntryBits == 6) {
+                        S.fill[w][nfill] = (e << 26) | wpr[j][l];
+                    } else {
+                        S.fill[w][nfill] = wpr[j][l];
+                        S.fent[w][nfill] = (uint8_t)e;
+                    }
                     S.fkey[w][nfill] = full_key(j);
                     S.hkey[e] = 0ull;  // set by the copy below
                 }
@@ -488,7 +496,12 @@ __device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, fl
         for (uint32_t fi = 0; fi < nfill; ++fi) {
             const uint32_t f = S.fill[w][fi];
             const uint64_t fkey = S.fkey[w][fi];
-            const uint32_t e = S.fent[w][fi], ps = f >> 8, len = f & 0xffu;
+            uint32_t e;
+            if constexpr (Tab::kEntryBits == 6)
+                e = f >> 26;
+            else
+                e = S.fent[w][fi];
+            const uint32_t ps = (f >> 8) & kLeadPosMask, len = f & 0xffu;
             float4 x[kPiece / 32];
             uint32_t lw[kPiece / 32];
 #pragma unroll
@@ -500,7 +513,7 @@ __device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, fl
 #pragma unroll
             for (int j = 0; j < kPiece / 32; ++j) {
                 const uint32_t i = lane + 32 * j, ri = i < len ? i : len - 1;
-                const uint32_t ll = lead_pos_leader<KD>(lead_loc_worker<KD>(lw[j])) | (ri << 7) | e;
+                const uint32_t ll = lead_pos_leader<KD, HPW>(lead_loc_worker<KD>(lw[j])) | (ri << Tab::kEntryBits) | e;
                 s_pt[e * kPiece + i] = x[j];
                 s_lw[e * kPiece + i] = ll;
                 const uint64_t kk = ((uint64_t)(__float_as_uint(x[j].w) | 0x80000000u) << 32) | lw[j];
@@ -565,15 +578,16 @@ __device__ __forceinline__ void lead_worker(const LeadArgs& a, LeadShared& S, fl
 
 // The leader warp on one cloud: per epoch, emit samples from the hot table
 // while its best key beats T.  Reaches lead_bar() as often as lead_worker.
-template <int D, bool FMA, bool KD>
-__device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, float4* s_pt, uint32_t* s_lw,
+template <int D, bool FMA, bool KD, int HPW>
+__device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared<HPW>& S, float4* s_pt, uint32_t* s_lw,
                                             const LeadCloud& cc, unsigned long long& tested,
                                             unsigned long long& touched) {
     const uint32_t lane = threadIdx.x & 31;
-    const bool has1 = lane + 32 < (uint32_t)kLeadHot, has2 = lane + 64 < (uint32_t)kLeadHot;
+    using Tab = LeadTable<HPW>;
+    const bool has1 = lane + 32 < (uint32_t)Tab::kHot, has2 = Tab::kThree && lane + 64 < (uint32_t)Tab::kHot;
     S.hkey[lane] = 0ull;  // every entry starts empty
     S.hkey[lane + 32] = 0ull;
-    S.hkey[lane + 64] = 0ull;
+    if constexpr (Tab::kThree) S.hkey[lane + 64] = 0ull;
     if (lane == 0) S.stall = 0;
     lead_bar();  // the workers' first reference
 
@@ -583,23 +597,29 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
         lead_bar();                 // the hot table is ready
         // T in leader format: the position decides ties, the rest is all ones
         uint64_t Tb = warp_max_key(lane < (uint32_t)kLeadWorkers ? S.T[lane] : 0ull);
-        if (Tb) Tb = (Tb & 0xffffffff00000000ull) | lead_pos_leader<KD>(lead_loc_worker<KD>((uint32_t)Tb)) | 0x3fffu;
+        if (Tb) Tb = (Tb & 0xffffffff00000000ull) | lead_pos_leader<KD, HPW>(lead_loc_worker<KD>((uint32_t)Tb)) |
+                       ((1u << Tab::kPosShift) - 1);
         uint64_t k0 = S.hkey[lane], k1 = has1 ? S.hkey[lane + 32] : 0ull, k2 = has2 ? S.hkey[lane + 64] : 0ull;
         const float4 l0 = S.hlo[lane], h0 = S.hhi[lane];
         const float4 l1 = has1 ? S.hlo[lane + 32] : make_float4(INFINITY, INFINITY, INFINITY, 0.0f);
         const float4 h1 = has1 ? S.hhi[lane + 32] : make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
         const float4 l2 = has2 ? S.hlo[lane + 64] : make_float4(INFINITY, INFINITY, INFINITY, 0.0f);
         const float4 h2 = has2 ? S.hhi[lane + 64] : make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
+        const float lo0[3] = {l0.x, l0.y, l0.z}, hi0[3] = {h0.x, h0.y, h0.z};
+        const float lo1[3] = {l1.x, l1.y, l1.z}, hi1[3] = {h1.x, h1.y, h1.z};
+        const float lo2[3] = {l2.x, l2.y, l2.z}, hi2[3] = {h2.x, h2.y, h2.z};
         bool mod0 = false, mod1 = false, mod2 = false;
         uint32_t s = 0;
-        auto max3 = [](uint64_t x, uint64_t y, uint64_t z) {
-            const uint64_t m = x > y ? x : y;
-            return m > z ? m : z;
+        // this lane's largest entry key
+        auto lane_max = [&]() {
+            const uint64_t m = k0 > k1 ? k0 : k1;
+            if constexpr (Tab::kThree) return m > k2 ? m : k2;
+            return m;
         };
-        uint64_t wk = warp_max_key(max3(k0, k1, k2));  // the best hot key (warp-uniform)
+        uint64_t wk = warp_max_key(lane_max());  // the best hot key (warp-uniform)
         while (!a.mute && emitted < cc.K && s < (uint32_t)kLeadRefs) {
             if (wk <= Tb) break;
-            const uint32_t e = (uint32_t)wk & 127u, rec = ((uint32_t)wk >> 7) & 127u;
+            const uint32_t e = (uint32_t)wk & ((1u << Tab::kEntryBits) - 1), rec = ((uint32_t)wk >> Tab::kEntryBits) & 127u;
             float4* const ep = s_pt + e * kPiece;
             const uint32_t* const el = s_lw + e * kPiece;
             const float4 r = ep[rec];
@@ -613,10 +633,10 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
                 w[j] = el[lane + 32 * j];
             }
             // publish (every lane stores the same values: no branch)
-            S.outq[s] = lead_loc_leader<KD>((uint32_t)wk);
+            S.outq[s] = lead_loc_leader<KD, HPW>((uint32_t)wk);
             S.ref[s] = r;
             st_release_cta_shared(&S.nref, s + 1);
-            tested += lane == 0 ? kLeadHot : 0u;
+            tested += lane == 0 ? (uint32_t)Tab::kHot : 0u;
             touched += lane == 0 ? kPiece : 0u;
             ++emitted;
             ++s;
@@ -624,9 +644,10 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
             // recompute (branch-free, so they share its basic block)
             const bool o0 = lane != e, o1 = lane + 32 != e, o2 = lane + 64 != e;
             const uint64_t x0 = o0 ? k0 : 0ull, x1 = o1 ? k1 : 0ull, x2 = o2 ? k2 : 0ull;
-            const bool d0 = (x0 != 0) & (lead_box_bound4<D, FMA>(l0, h0, r) < key_dist(x0));
-            const bool d1 = (x1 != 0) & (lead_box_bound4<D, FMA>(l1, h1, r) < key_dist(x1));
-            const bool d2 = (x2 != 0) & (lead_box_bound4<D, FMA>(l2, h2, r) < key_dist(x2));
+            const float rv[3] = {r.x, r.y, r.z};
+            const bool d0 = (x0 != 0) & (box_bound<D, FMA>(lo0, hi0, rv) < key_dist(x0));
+            const bool d1 = (x1 != 0) & (box_bound<D, FMA>(lo1, hi1, rv) < key_dist(x1));
+            const bool d2 = Tab::kThree && (x2 != 0) & (box_bound<D, FMA>(lo2, hi2, rv) < key_dist(x2));
             // the winner's recompute
             uint32_t bh[kPiece / 32];
 #pragma unroll
@@ -646,7 +667,7 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
             // reductions issue side by side.
             uint32_t ch = (uint32_t)(x0 >> 32), cl = (uint32_t)x0;
             lead_pmax(ch, cl, (uint32_t)(x1 >> 32), (uint32_t)x1);
-            lead_pmax(ch, cl, (uint32_t)(x2 >> 32), (uint32_t)x2);
+            if constexpr (Tab::kThree) lead_pmax(ch, cl, (uint32_t)(x2 >> 32), (uint32_t)x2);
             lead_pmax(ch, cl, bh[0], w[0]);
             const uint32_t ah = __reduce_max_sync(kFull, ch);
             const uint32_t nh = __reduce_max_sync(kFull, bh[0]);
@@ -655,10 +676,12 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
             const uint64_t nk = ((uint64_t)nh << 32) | nl;
             k0 = o0 ? k0 : nk;
             k1 = o1 ? k1 : nk;
-            k2 = o2 ? k2 : nk;
             mod0 |= !o0;
             mod1 |= !o1;
-            mod2 |= !o2;
+            if constexpr (Tab::kThree) {
+                k2 = o2 ? k2 : nk;
+                mod2 |= !o2;
+            }
             if (__any_sync(kFull, d0 || d1 || d2)) {
                 // every other hot entry whose box is nearer than its key
                 uint32_t m = __ballot_sync(kFull, d0);
@@ -683,18 +706,21 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
                         mod1 = true;
                     }
                 }
-                m = __ballot_sync(kFull, d2);
-                while (m) {
-                    const uint32_t l = __ffs(m) - 1;
-                    m &= m - 1;
-                    touched += lane == 0 ? kPiece : 0u;
-                    const uint64_t k = lead_update_hot<D, FMA>(s_pt + (l + 64) * kPiece, s_lw + (l + 64) * kPiece, r);
-                    if (lane == l) {
-                        k2 = k;
-                        mod2 = true;
+                if constexpr (Tab::kThree) {
+                    m = __ballot_sync(kFull, d2);
+                    while (m) {
+                        const uint32_t l = __ffs(m) - 1;
+                        m &= m - 1;
+                        touched += lane == 0 ? kPiece : 0u;
+                        const uint64_t k =
+                            lead_update_hot<D, FMA>(s_pt + (l + 64) * kPiece, s_lw + (l + 64) * kPiece, r);
+                        if (lane == l) {
+                            k2 = k;
+                            mod2 = true;
+                        }
                     }
                 }
-                wk = warp_max_key(max3(k0, k1, k2));
+                wk = warp_max_key(lane_max());
             } else {
                 wk = ((uint64_t)ah << 32) | al;  // nothing else changed
             }
@@ -716,9 +742,11 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
             S.hkey[lane + 32] = k1;
             if (mod1) S.hmod[lane + 32] = 1;
         }
-        if (has2) {
-            S.hkey[lane + 64] = k2;
-            if (mod2) S.hmod[lane + 64] = 1;
+        if constexpr (Tab::kThree) {
+            if (has2) {
+                S.hkey[lane + 64] = k2;
+                if (mod2) S.hmod[lane + 64] = 1;
+            }
         }
         if (mod0) S.hmod[lane] = 1;
         if (lane == 0) {
@@ -731,12 +759,13 @@ __device__ __forceinline__ void lead_leader(const LeadArgs& a, LeadShared& S, fl
     }
 }
 
-template <int D, bool FMA, bool KD>
+template <int D, bool FMA, bool KD, int HPW>
 __global__ void __launch_bounds__(kLeadThreads, 1) lead_sample(LeadArgs a) {
+    constexpr uint32_t kHotPoints = (uint32_t)LeadTable<HPW>::kHot * kPiece;
     extern __shared__ __align__(16) unsigned char s_dyn[];
-    __shared__ LeadShared S;
-    float4* s_pt = reinterpret_cast<float4*>(s_dyn);                      // [kLeadHotPoints]
-    uint32_t* s_lw = reinterpret_cast<uint32_t*>(s_pt + kLeadHotPoints);  // [kLeadHotPoints]
+    __shared__ LeadShared<HPW> S;
+    float4* s_pt = reinterpret_cast<float4*>(s_dyn);                  // [kHotPoints]
+    uint32_t* s_lw = reinterpret_cast<uint32_t*>(s_pt + kHotPoints);  // [kHotPoints]
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     unsigned long long tested = 0, touched = 0;
     bool gave_up = false;
@@ -765,9 +794,9 @@ __global__ void __launch_bounds__(kLeadThreads, 1) lead_sample(LeadArgs a) {
             if (a.out_pts && tid < D) a.out_pts[cc.ooff * D + tid] = tid == 0 ? r.x : tid == 1 ? r.y : r.z;
         }
         if (warp == 0)
-            lead_leader<D, FMA, KD>(a, S, s_pt, s_lw, cc, tested, touched);
+            lead_leader<D, FMA, KD, HPW>(a, S, s_pt, s_lw, cc, tested, touched);
         else
-            lead_worker<D, FMA, KD>(a, S, s_pt, s_lw, cc, r, warp - 1, tested, touched, gave_up);
+            lead_worker<D, FMA, KD, HPW>(a, S, s_pt, s_lw, cc, r, warp - 1, tested, touched, gave_up);
         if (S.stall && tid == 0) atomicOr(a.err, kErrBadIndex);
         lead_bar();  // the leader's output writes are visible to the CTA
         if (KD) {
