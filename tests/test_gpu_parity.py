@@ -380,7 +380,7 @@ def test_one_cta_sampler_epochs_with_ties(kind, mode):
             np.testing.assert_array_equal(fps.fps_sampling(p, k, s), ORACLE.fps(p, k, [s], mode))
 
 
-_LOCKSTEP_CHILD = r"""
+_BATCH_CHILD = r"""
 import sys
 import numpy as np
 import fpsample as fps
@@ -405,7 +405,34 @@ def test_lockstep_one_cta_sampler_d3(mode, tmp_path):
     np.savez(inp, clouds=np.array(clouds, dtype=object), ks=ks, hs=hs, ss=ss, mode=mode)
     env = dict(os.environ, FPSGPU_ONECTA_SAMPLER="lockstep")
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    subprocess.run([sys.executable, "-c", _LOCKSTEP_CHILD, str(inp), str(out)], env=env, cwd=root,
+    subprocess.run([sys.executable, "-c", _BATCH_CHILD, str(inp), str(out)], env=env, cwd=root,
+                   check=True, timeout=600)
+    got = np.load(out, allow_pickle=True)
+    for p, k, h, s, g in zip(clouds, ks, hs, ss, got):
+        np.testing.assert_array_equal(g, ORACLE.kdline(p, k, h, s, mode))
+
+
+@pytest.mark.parametrize("hot", ["5", "7"])
+def test_both_hot_table_widths_on_every_cloud_size(mode, hot, tmp_path):
+    """The leader/worker sampler's two tables (55 and 77 hot pieces; a launch
+    takes the wide one when it holds a cloud of 512 pieces or more) forced with
+    FPSGPU_LEAD_HOT for clouds of every size, ties and a two-point cloud
+    included, against the oracle (a child process: the setting is read
+    once per process)."""
+    import os
+    import subprocess
+    import sys
+
+    clouds, ks, hs, ss = _batch_clouds(37, 14, 300, 120000, 3)
+    clouds.append(np.array([[0, 0, 0], [1, 2, 3]], np.float32))  # the smallest cloud h = 1 allows
+    ks.append(2)
+    hs.append(1)
+    ss.append(1)
+    inp, out = tmp_path / "in.npz", tmp_path / "out.npy"
+    np.savez(inp, clouds=np.array(clouds, dtype=object), ks=ks, hs=hs, ss=ss, mode=mode)
+    env = dict(os.environ, FPSGPU_LEAD_HOT=hot)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.run([sys.executable, "-c", _BATCH_CHILD, str(inp), str(out)], env=env, cwd=root,
                    check=True, timeout=600)
     got = np.load(out, allow_pickle=True)
     for p, k, h, s, g in zip(clouds, ks, hs, ss, got):
